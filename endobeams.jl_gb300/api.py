@@ -1,0 +1,486 @@
+"""Host API mirroring EndoBeams.jl's public interface (src/EndoBeams.jl:37-43).
+
+The constructors keep the reference's names, argument order and 1-based
+indexing for connectivity and degrees of freedom, so a script written for
+the Julia package reads the same here:
+
+    nodes = NodesBeams(X, u0, ud0, udd0, w0, wd0, wdd0)
+    beams = Beams(nodes, connectivity, E, nu, rho, radius, damping)
+    conf  = BeamsConfiguration(nodes, beams, Loads(ConcentratedForce(f, [27])),
+                               BoundaryConditions(Encastre(range(1, 7)), 6 * n))
+    params = SimulationParams(alpha=a, beta=b, gamma=g, ...)
+    run_simulation(conf, params)          # run_simulation! (src/run_simulation.jl:1)
+
+Every step runs on the GPU through libendobeams_gb300 (there is no CPU
+path); ``run_simulations`` runs many independent configurations in one
+batched handle.  VTK output (src/IO/*) is not produced.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, f64, i32, i64, ptr
+
+# ------------------------------------------------------------------ configuration objects
+
+
+def _dofs(x) -> np.ndarray:
+    """1-based Int / UnitRange / Vector of DOFs -> sorted 0-based int64 array (order kept)."""
+    if isinstance(x, (int, np.integer)):
+        return np.array([int(x) - 1], np.int64)
+    return np.asarray(list(x), dtype=np.int64) - 1
+
+
+class NodesBeams:
+    """NodesBeams(X, u⁰, u̇⁰, ü⁰, w⁰, ẇ⁰, ẅ⁰, plane=nothing, R=nothing) (def_node_beam.jl:55-90)."""
+
+    def __init__(self, X, u0=None, ud0=None, udd0=None, w0=None, wd0=None, wdd0=None, plane=None, R=None):
+        self.X0 = f64(X).reshape(-1, 3)
+        n = self.X0.shape[0]
+        z = lambda a: f64(a).reshape(n, 3) if a is not None else np.zeros((n, 3))
+        self.u, self.ud, self.udd = z(u0), z(ud0), z(udd0)
+        self.w, self.wd, self.wdd = z(w0), z(wd0), z(wdd0)
+        if R is None:
+            self.R = np.tile(np.eye(3).flatten(order="F"), (n, 1))
+        else:
+            R = f64(R)
+            self.R = R.reshape(n, 9) if R.ndim != 3 else np.stack([r.flatten(order="F") for r in R])
+        self.dR = np.tile(np.eye(3).flatten(order="F"), (n, 1))
+        self.plane = plane
+        # state at the last converged step (uⁿ, u̇ⁿ, ... of NodeBeam)
+        self.un, self.udn, self.uddn = self.u.copy(), self.ud.copy(), self.udd.copy()
+        self.wn, self.wdn, self.wddn = self.w.copy(), self.wd.copy(), self.wdd.copy()
+        self.Rn, self.dRn = self.R.copy(), self.dR.copy()
+
+    def __len__(self):
+        return self.X0.shape[0]
+
+
+class Beams:
+    """Beams(nodes, connectivity, E, ν, ρ, radius, damping, Rₑ⁰=nothing) (def_beam.jl:102-142).
+
+    ``connectivity`` is 1-based like the reference (rows of node pairs)."""
+
+    def __init__(self, nodes: NodesBeams, connectivity, E, nu, rho, radius, damping, Re0=None):
+        conn = np.asarray([tuple(c) for c in connectivity] if not isinstance(connectivity, np.ndarray) else connectivity)
+        self.conn = i64(conn).reshape(-1, 2) - 1
+        ne = self.conn.shape[0]
+        bc = lambda x: np.broadcast_to(np.asarray(x, float), (ne,)).copy()
+        self.E, self.nu, self.rho, self.radius, self.damping = bc(E), bc(nu), bc(rho), bc(radius), bc(damping)
+        self.Re0 = None if Re0 is None else f64(Re0).reshape(ne, 9)
+
+    def __len__(self):
+        return self.conn.shape[0]
+
+
+@dataclass
+class ConcentratedForce:
+    """ConcentratedForce(force_function(t, dof), loaded_dofs) (def_bcs_and_loads.jl:66-77); dofs 1-based."""
+    force_function: Callable[[float, int], float]
+    loaded_dofs: Sequence[int]
+
+
+@dataclass
+class Loads:
+    concentrated_force: Optional[ConcentratedForce] = None
+
+
+@dataclass
+class Encastre:
+    blocked_dofs: Sequence[int]
+
+
+@dataclass
+class ImposedDisplacement:
+    displaced_dofs: Sequence[int]
+    imposed_displacements_function: Callable[[float], float]
+
+
+class BoundaryConditions:
+    """BoundaryConditions constructors of def_bcs_and_loads.jl:86-127 (dofs 1-based)."""
+
+    def __init__(self, *args):
+        ndofs = int(args[-1])
+        bcs = args[:-1]
+        enc = next((b for b in bcs if isinstance(b, Encastre)), None)
+        imp = next((b for b in bcs if isinstance(b, ImposedDisplacement)), None)
+        fixed = []
+        if enc is not None:
+            fixed += list(_dofs(enc.blocked_dofs))
+        disp = list(_dofs(imp.displaced_dofs)) if imp is not None else []
+        if enc is not None and imp is not None:
+            fixed = sorted(disp + fixed)
+        elif imp is not None:
+            fixed = disp
+        self.fixed_dofs = np.asarray(fixed, np.int64)
+        mask = np.ones(ndofs, bool)
+        mask[self.fixed_dofs] = False
+        self.free_dofs = np.nonzero(mask)[0]
+        self.displaced_indices = np.asarray([i for i, d in enumerate(self.fixed_dofs) if d in set(disp)], np.int64)
+        self.imposed_displacements = np.zeros(len(self.fixed_dofs))
+        self.imposed_displacements_function = imp.imposed_displacements_function if imp is not None else None
+
+
+class BeamsConfiguration:
+    """BeamsConfiguration(nodes, beams, loads, bcs) (def_configurations.jl:15-26)."""
+
+    def __init__(self, nodes: NodesBeams, beams: Beams, loads: Optional[Loads] = None,
+                 bcs: Optional[BoundaryConditions] = None):
+        self.nodes, self.beams, self.loads = nodes, beams, loads
+        self.ndofs = 6 * len(nodes)
+        self.bcs = bcs if bcs is not None else BoundaryConditions(self.ndofs)
+
+
+@dataclass
+class InteractionProperties:
+    """InteractionProperties(kₙ, μ, εᵗ, ηₙ, kₜ, ηₜ, u̇ₛ) (def_interactions.jl:6-14); kₜ, ηₜ, u̇ₛ are unused."""
+    kn: float
+    mu: float
+    eps_t: float
+    eta_n: float
+    kt: float = 0.0
+    eta_t: float = 0.0
+    u_s: float = 0.0
+
+
+@dataclass
+class SphereSurface:
+    center: Sequence[float]
+    radius: float
+
+
+@dataclass
+class PlaneSurface:
+    """Declared by the reference (def_interactions.jl:24-27) without a gap method; not usable there either."""
+    position: float
+    axis: str
+
+
+class DiscreteSignedDistanceField:
+    """DiscreteSignedDistanceField(filename, inside) (def_interactions.jl:67-82).
+
+    The grid is kept as given (x fastest); the quadratic B-spline prefilter
+    runs in the library.  ``from_grid`` builds one from an array."""
+
+    def __init__(self, filename: Optional[str] = None, inside: bool = True, flag_load_from_file_iterative=False,
+                 *, values=None, origin=None, spacing=None):
+        if filename is not None:
+            dims, spacing, origin, values = read_vtk_sdf(filename)
+            values = np.asarray(values, float).reshape(dims[2], dims[1], dims[0])
+        self.values = f64(values)  # [k, j, i]
+        nz, ny, nx = self.values.shape
+        self.dims = (nx, ny, nz)
+        self.origin = tuple(float(x) for x in origin)
+        self.spacing = tuple(float(x) for x in np.broadcast_to(np.asarray(spacing, float), (3,)))
+        self.inside = bool(inside)
+        ends = [self.origin[a] + (self.dims[a] - 1) * self.spacing[a] for a in range(3)]
+        self.dom = (self.origin[0], ends[0], self.origin[1], ends[1], self.origin[2], ends[2])
+
+    @classmethod
+    def from_grid(cls, values, origin, spacing, inside=True):
+        return cls(None, inside, values=values, origin=origin, spacing=spacing)
+
+
+def read_vtk_sdf(filename: str):
+    """Legacy-VTK structured-points reader with the layout of read_vtk_sdf (read_input_files.jl:154-195)."""
+    with open(filename) as fh:
+        for _ in range(4):
+            fh.readline()
+        dims = [int(x) for x in fh.readline().split()[1:4]]
+        spacing = [float(x) for x in fh.readline().split()[1:4]]
+        origin = [float(x) for x in fh.readline().split()[1:4]]
+        n = int(fh.readline().split()[1])
+        fh.readline()
+        fh.readline()
+        vals = []
+        while len(vals) < n:
+            vals += [float(x) for x in fh.readline().split()]
+    return dims, spacing, origin, np.asarray(vals[:n])
+
+
+class BeamElementSurface:
+    """BeamElementSurface(contact_beams) (def_interactions.jl:172-184); 1-based element ids or a connectivity matrix."""
+
+    def __init__(self, x):
+        a = np.asarray(x)
+        if a.ndim == 2:
+            self.contact_beams = np.arange(a.shape[0], dtype=np.int64)
+        else:
+            self.contact_beams = np.asarray(list(x), np.int64) - 1
+
+
+@dataclass
+class RigidInteraction:
+    master: object
+    slave: BeamElementSurface
+    properties: InteractionProperties
+
+
+@dataclass
+class SimulationParams:
+    """SimulationParams (def_params.jl:1-35) plus the linear-solver knobs of this implementation."""
+    alpha: float
+    beta: float
+    gamma: float
+    verbose: bool = False
+    record_timings: bool = False
+    output_dir: str = ""
+    initial_timestep: float = 1e-2
+    min_timestep: float = 1e-10
+    max_timestep: float = 1e-2
+    output_timestep: float = 1e-4
+    simulation_end_time: float = 1e-2
+    accelerate_after_success_it: int = 4
+    stop_on_energy_threshold: bool = False
+    energy_threshold: float = 0.0
+    tcompt_max: float = 1800.0
+    stop_long_simulation: bool = False
+    tolerance_residual: float = 1e-5
+    tolerance_displacement: float = 1e-5
+    max_iterations: int = 20
+    nG_beams: int = 3
+    wG_beams: tuple = (5 / 9, 8 / 9, 5 / 9)
+    zG_beams: tuple = (-math.sqrt(3 / 5), 0.0, math.sqrt(3 / 5))
+    # linear solver (replaces PARDISO)
+    precision: str = "fp64"          # "fp64" | "mixed"
+    krylov_restart: int = 64
+    krylov_max_iter: int = 4000
+    linear_tol: float = 1e-10
+    inner_tol: float = 1e-4
+    max_refinements: int = 60
+    threads_per_sim: int = 0
+
+    def to_c(self) -> _lib.EbParams:
+        p = _lib.default_params()
+        p.alpha, p.beta, p.gamma = self.alpha, self.beta, self.gamma
+        p.tolerance_residual, p.tolerance_displacement = self.tolerance_residual, self.tolerance_displacement
+        p.max_iterations = int(self.max_iterations)
+        for i in range(3):
+            p.gauss_w[i] = self.wG_beams[i]
+            p.gauss_z[i] = self.zG_beams[i]
+        p.precision = _lib.EB_PREC_MIXED if self.precision == "mixed" else _lib.EB_PREC_FP64
+        p.krylov_restart = int(self.krylov_restart)
+        p.krylov_max_iter = int(self.krylov_max_iter)
+        p.linear_tol = float(self.linear_tol)
+        p.inner_tol = float(self.inner_tol)
+        p.max_refinements = int(self.max_refinements)
+        p.threads_per_sim = int(self.threads_per_sim)
+        return p
+
+
+# ------------------------------------------------------------------ the batched engine
+
+class GpuSimulations:
+    """One device handle holding many independent configurations.
+
+    Methods map one-to-one onto the C ABI: ``step`` is solve_step_dynamics!,
+    ``commit``/``rollback`` are update_converged!/update_not_converged!."""
+
+    def __init__(self, confs: Sequence[BeamsConfiguration], params: SimulationParams,
+                 inters: Optional[Sequence[Optional[RigidInteraction]]] = None):
+        self.L = _lib.load()
+        self.confs = list(confs)
+        self.params = params
+        self.inters = list(inters) if inters is not None else [None] * len(self.confs)
+        self._keep = []
+        descs = (_lib.EbSimDesc * len(self.confs))()
+        for s, (conf, inter) in enumerate(zip(self.confs, self.inters)):
+            self._fill(descs[s], conf, inter)
+        self.cparams = params.to_c()
+        h = C.c_void_p()
+        check(self.L.eb_create(C.byref(self.cparams), len(self.confs), descs, C.byref(h)), "eb_create")
+        self.h = h
+        self.n = len(self.confs)
+        self._stats = (_lib.EbSimStats * self.n)()
+
+    def _k(self, a):
+        self._keep.append(a)
+        return a
+
+    def _fill(self, d: _lib.EbSimDesc, conf: BeamsConfiguration, inter: Optional[RigidInteraction]):
+        nd, bm = conf.nodes, conf.beams
+        d.n_nodes, d.n_elem = len(nd), len(bm)
+        for name in ("X0", "u", "ud", "udd", "w", "wd", "wdd"):
+            setattr(d, name, ptr(self._k(f64(getattr(nd, name)))))
+        d.R = ptr(self._k(f64(nd.R)))
+        d.conn = ptr(self._k(i64(bm.conn)), C.c_int64)
+        for name in ("E", "nu", "rho", "radius", "damping"):
+            setattr(d, name, ptr(self._k(f64(getattr(bm, name)))))
+        d.Re0 = ptr(self._k(f64(bm.Re0))) if bm.Re0 is not None else None
+        fixed = i64(conf.bcs.fixed_dofs)
+        d.n_fixed = len(fixed)
+        d.fixed_dofs = ptr(self._k(fixed), C.c_int64) if len(fixed) else None
+        cf = conf.loads.concentrated_force if conf.loads is not None else None
+        if cf is not None and len(cf.loaded_dofs):
+            ld = _dofs(cf.loaded_dofs)
+            d.n_loaded = len(ld)
+            d.loaded_dofs = ptr(self._k(i64(ld)), C.c_int64)
+            d.fext0 = ptr(self._k(f64([cf.force_function(0.0, int(i) + 1) for i in ld])))
+        if inter is not None:
+            m, pr = inter.master, inter.properties
+            d.kn, d.mu, d.eps_t, d.eta_n = pr.kn, pr.mu, pr.eps_t, pr.eta_n
+            ce = i64(inter.slave.contact_beams)
+            d.n_contact_elems = len(ce)
+            d.contact_elems = ptr(self._k(ce), C.c_int64)
+            if isinstance(m, SphereSurface):
+                d.surface = _lib.EB_SURFACE_SPHERE
+                for i in range(3):
+                    d.sphere_center[i] = float(m.center[i])
+                d.sphere_radius = float(m.radius)
+            elif isinstance(m, DiscreteSignedDistanceField):
+                d.surface = _lib.EB_SURFACE_SDF
+                for i in range(3):
+                    d.sdf_dims[i] = m.dims[i]
+                    d.sdf_origin[i] = m.origin[i]
+                    d.sdf_spacing[i] = m.spacing[i]
+                d.sdf_values = ptr(self._k(f64(m.values)))
+                d.sdf_inside = 1 if m.inside else 0
+            else:
+                raise NotImplementedError(f"surface {type(m).__name__} has no gap function")
+
+    # ---- per-step inputs (update_loads!, update_boundary_conditions!)
+    def set_time(self, s: int, t: float):
+        conf = self.confs[s]
+        cf = conf.loads.concentrated_force if conf.loads is not None else None
+        if cf is not None and len(cf.loaded_dofs):
+            vals = f64([cf.force_function(t, int(i) + 1) for i in _dofs(cf.loaded_dofs)])
+            check(self.L.eb_set_loads(self.h, s, ptr(vals)), "eb_set_loads")
+        bcs = conf.bcs
+        if bcs.imposed_displacements_function is not None and len(bcs.displaced_indices):
+            bcs.imposed_displacements[bcs.displaced_indices] = bcs.imposed_displacements_function(t)
+            check(self.L.eb_set_imposed(self.h, s, ptr(f64(bcs.imposed_displacements))), "eb_set_imposed")
+
+    def step(self, dt, active=None):
+        dt = f64(np.broadcast_to(np.asarray(dt, float), (self.n,)))
+        act = None if active is None else i32(active)
+        k = np.zeros(self.n, np.int32)
+        st = np.zeros(self.n, np.int32)
+        check(self.L.eb_step(self.h, ptr(dt), ptr(act, C.c_int32) if act is not None else None,
+                             ptr(k, C.c_int32), ptr(st, C.c_int32)), "eb_step")
+        return k, st
+
+    def commit(self, mask=None):
+        m = None if mask is None else i32(mask)
+        check(self.L.eb_commit(self.h, ptr(m, C.c_int32) if m is not None else None), "eb_commit")
+
+    def rollback(self, mask=None):
+        m = None if mask is None else i32(mask)
+        check(self.L.eb_rollback(self.h, ptr(m, C.c_int32) if m is not None else None), "eb_rollback")
+
+    def state(self, s: int, at_n: bool = False) -> dict:
+        n = len(self.confs[s].nodes)
+        out = {k: np.zeros((n, 3)) for k in ("u", "ud", "udd", "w", "wd", "wdd")}
+        out["R"] = np.zeros((n, 9))
+        out["dR"] = np.zeros((n, 9))
+        f = self.L.eb_get_state_n if at_n else self.L.eb_get_state
+        check(f(self.h, s, *(ptr(out[k]) for k in ("u", "ud", "udd", "w", "wd", "wdd", "R", "dR"))), "eb_get_state")
+        return out
+
+    def forces(self, s: int) -> dict:
+        N = 6 * len(self.confs[s].nodes)
+        out = {k: np.zeros(N) for k in ("Tint", "Tk", "Tc")}
+        check(self.L.eb_get_forces(self.h, s, ptr(out["Tint"]), ptr(out["Tk"]), ptr(out["Tc"])), "eb_get_forces")
+        return out
+
+    def stats(self):
+        check(self.L.eb_get_stats(self.h, self._stats), "eb_get_stats")
+        return [{f: getattr(x, f) for f, _ in _lib.EbSimStats._fields_} for x in self._stats]
+
+    def sync_nodes(self):
+        """Copies the device state back into the NodesBeams objects (uⁿ… and u…)."""
+        for s, conf in enumerate(self.confs):
+            nd = conf.nodes
+            a = self.state(s, at_n=False)
+            b = self.state(s, at_n=True)
+            nd.u, nd.ud, nd.udd, nd.w, nd.wd, nd.wdd, nd.R, nd.dR = (a[k] for k in ("u", "ud", "udd", "w", "wd", "wdd", "R", "dR"))
+            nd.un, nd.udn, nd.uddn, nd.wn, nd.wdn, nd.wddn, nd.Rn, nd.dRn = (b[k] for k in ("u", "ud", "udd", "w", "wd", "wdd", "R", "dR"))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.eb_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class RunResult:
+    steps: List[int]
+    ks: List[List[int]]
+    t: List[float]
+    wall_s: float
+    newton_iterations: List[int] = field(default_factory=list)
+    krylov_iterations: List[int] = field(default_factory=list)
+
+
+def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Optional[int] = None,
+                    engine: Optional[GpuSimulations] = None, on_step=None) -> RunResult:
+    """The time loop of run_simulation! (run_simulation.jl:170-244) for many
+    configurations at once: each keeps its own t, Δt and success counter, and
+    all simulations still running advance together in one batched step."""
+    eng = engine or GpuSimulations(confs, params, inters)
+    p = params
+    S = eng.n
+    t = np.zeros(S)
+    dt = np.full(S, float(p.initial_timestep))
+    succ = np.zeros(S, int)
+    step = np.ones(S, int)
+    ks = [[] for _ in range(S)]
+    newton = np.zeros(S, int)
+    krylov = np.zeros(S, int)
+    t0 = time.perf_counter()
+    while True:
+        running = (p.simulation_end_time - t > 1.0e-10)
+        if max_steps is not None:
+            running &= step <= max_steps
+        if not running.any():
+            break
+        dt_used = dt.copy()
+        for s in np.nonzero(running)[0]:
+            eng.set_time(int(s), float(t[s] + dt_used[s]))  # update_loads! / update_boundary_conditions!
+        k, _ = eng.step(dt_used, running.astype(np.int32))
+        st = eng.stats()
+        for s in np.nonzero(running)[0]:
+            newton[s] += st[s]["newton_iterations"]
+            krylov[s] += st[s]["krylov_iterations"]
+        failed = running & (k > p.max_iterations)       # run_simulation.jl:187-203
+        ok = running & ~failed
+        if failed.any():
+            dt[failed] = dt[failed] / 2
+            if (dt[failed] < p.min_timestep).any():
+                raise RuntimeError("Simulation aborted: Δt < min_timestep")
+            eng.rollback(failed.astype(np.int32))
+            succ[failed] = 0
+        succ[ok] += 1
+        grow = ok & (succ >= p.accelerate_after_success_it) & (k <= 8)  # :211-216
+        dt[grow] = np.minimum(dt[grow] * 1.5, p.max_timestep)
+        succ[grow] = 0
+        if ok.any():
+            eng.commit(ok.astype(np.int32))              # update_converged!, :232
+        for s in np.nonzero(ok)[0]:
+            ks[s].append(int(k[s]))
+        t[ok] = t[ok] + dt_used[ok]
+        step[ok] += 1
+        if on_step is not None:
+            on_step(eng, ok, k)
+    wall = time.perf_counter() - t0
+    eng.sync_nodes()
+    return RunResult(steps=list(step - 1), ks=ks, t=list(t), wall_s=wall, newton_iterations=list(newton),
+                     krylov_iterations=list(krylov))
+
+
+def run_simulation(conf: BeamsConfiguration, params: SimulationParams, inter: Optional[RigidInteraction] = None,
+                   max_steps: Optional[int] = None) -> RunResult:
+    """run_simulation!(conf, params, inter) (src/run_simulation.jl:133-251) on the GPU."""
+    return run_simulations([conf], params, [inter], max_steps=max_steps)

@@ -1,0 +1,779 @@
+// C ABI of endobeams_gb300 (declared in include/endobeams_gb300.h): handle
+// construction, the HHT step orchestration and the testing entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/endobeams_gb300.h"
+#include "eb_gmres.cuh"
+#include "eb_internal.cuh"
+
+using namespace eb;
+
+namespace {
+
+thread_local char g_err[1024] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(EB_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// Device allocation list owned by a handle.
+struct Arena {
+  std::vector<void*> ptrs;
+  size_t bytes = 0;
+  ~Arena() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  cudaError_t alloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e == cudaSuccess) {
+      ptrs.push_back(*p);
+      bytes += n * sizeof(T);
+      e = cudaMemset(*p, 0, n * sizeof(T));
+    }
+    return e;
+  }
+  template <typename T>
+  cudaError_t upload(T** p, const std::vector<T>& h) {
+    cudaError_t e = alloc(p, h.size());
+    if (e == cudaSuccess && !h.empty()) e = cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+  }
+};
+
+// ---------------------------------------------------------------- geometry helpers (host, FP64)
+
+// get_Rₑ⁰ (src/beams/def_beam.jl:163-186), column-major output
+void initial_frame(const double* X1, const double* X2, double* R) {
+  const double eps = 2.220446049250313e-16;
+  double d[3] = {X2[0] - X1[0], X2[1] - X1[1], X2[2] - X1[2]};
+  double l0 = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  double e[3] = {d[0] / l0, d[1] / l0, d[2] / l0};
+  double v[3] = {0.0, -e[2], e[1]};  // E1 × e
+  double s = std::sqrt(v[1] * v[1] + v[2] * v[2]);
+  double c = e[0];
+  for (int k = 0; k < 9; ++k) R[k] = 0.0;
+  if (c < -(1 - 2 * eps)) {
+    R[0] = -1; R[4] = 1; R[8] = -1;
+    return;
+  }
+  R[0] = 1; R[4] = 1; R[8] = 1;
+  if (c > (1 - 2 * eps)) return;
+  // I + S + (1-c)/s² S², S = skew(v)
+  double S[9] = {0, v[2], -v[1], -v[2], 0, v[0], v[1], -v[0], 0};  // column-major skew
+  double f = (1 - c) / (s * s);
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) {
+      double s2 = 0;
+      for (int q = 0; q < 3; ++q) s2 += S[i + 3 * q] * S[q + 3 * j];
+      R[i + 3 * j] += S[i + 3 * j] + f * s2;
+    }
+}
+
+// Quadratic B-spline prefilter with the even reflection at the cell edges
+// (c[0] = c[1], c[n+1] = c[n]): solves ⅛c[i-1] + ¾c[i] + ⅛c[i+1] = y[i]
+// along every grid line, axis by axis, into the padded coefficient grid.
+void prefilter_axis(double* c, const int64_t dims[3], int axis, std::vector<double>& work) {
+  const int64_t P[3] = {dims[0] + 2, dims[1] + 2, dims[2] + 2};
+  const int64_t stride = axis == 0 ? 1 : (axis == 1 ? P[0] : P[0] * P[1]);
+  const int64_t n = dims[axis];
+  // the other two axes: interior for axes not yet filtered, full padded range for filtered ones
+  int o1 = (axis + 1) % 3, o2 = (axis + 2) % 3;
+  auto lo = [&](int ax) { return ax < axis ? (int64_t)0 : (int64_t)1; };
+  auto hi = [&](int ax) { return ax < axis ? P[ax] : dims[ax] + 1; };
+  int64_t st[3] = {1, P[0], P[0] * P[1]};
+  work.resize(2 * n);
+  double* cp = work.data();
+  double* dp = cp + n;
+  for (int64_t b = lo(o2); b < hi(o2); ++b)
+    for (int64_t a = lo(o1); a < hi(o1); ++a) {
+      double* y = c + a * st[o1] + b * st[o2] + stride;  // first interior point
+      if (n > 1) {
+        // Thomas algorithm; diagonal 7/8 at both ends, 3/4 inside, off-diagonals 1/8
+        double m = 0.875;
+        cp[0] = 0.125 / m;
+        dp[0] = y[0] / m;
+        for (int64_t i = 1; i < n; ++i) {
+          const double di = (i == n - 1) ? 0.875 : 0.75;
+          m = di - 0.125 * cp[i - 1];
+          cp[i] = (i == n - 1) ? 0.0 : 0.125 / m;
+          dp[i] = (y[i * stride] - 0.125 * dp[i - 1]) / m;
+        }
+        y[(n - 1) * stride] = dp[n - 1];
+        for (int64_t i = n - 2; i >= 0; --i) y[i * stride] = dp[i] - cp[i] * y[(i + 1) * stride];
+      }
+      y[-stride] = y[0];
+      y[n * stride] = y[(n - 1) * stride];
+    }
+}
+
+std::vector<double> sdf_coefficients(const double* values, const int64_t dims[3], bool negate) {
+  const int64_t px = dims[0] + 2, py = dims[1] + 2, pz = dims[2] + 2;
+  std::vector<double> c((size_t)(px * py * pz), 0.0);
+  for (int64_t k = 0; k < dims[2]; ++k)
+    for (int64_t j = 0; j < dims[1]; ++j)
+      for (int64_t i = 0; i < dims[0]; ++i) {
+        double v = values[i + dims[0] * (j + dims[1] * k)];
+        c[(size_t)((i + 1) + px * ((j + 1) + py * (k + 1)))] = negate ? -v : v;
+      }
+  std::vector<double> work;
+  for (int ax = 0; ax < 3; ++ax) prefilter_axis(c.data(), dims, ax, work);
+  return c;
+}
+
+}  // namespace
+
+std::vector<double> eb_sdf_coefficients_host(const double* values, const int64_t dims[3], bool negate) {
+  return sdf_coefficients(values, dims, negate);
+}
+int eb_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
+// ---------------------------------------------------------------- handle
+struct eb_handle {
+  eb_params P;
+  int n_sims = 0;
+  cudaStream_t stream = nullptr;
+  Arena arena;
+  Dev d{};
+  Gauss3 gauss{};
+  std::vector<int64_t> node_off, elem_off, blk_off;
+  std::vector<int> has_contact;
+  bool any_contact = false;
+  // loads / imposed
+  std::vector<int64_t> load_off, fix_off;  // per-sim offsets into the flattened lists
+  std::vector<int64_t> load_dof, fix_dof;  // global dofs
+  int64_t* d_load_dof = nullptr;
+  int64_t* d_fix_dof = nullptr;
+  double* d_vals = nullptr;                // scratch for set_loads / set_imposed
+  // per-sim device arrays
+  int* d_mask = nullptr;
+  int* d_active = nullptr;
+  double *d_cK = nullptr, *d_cC = nullptr, *d_cM = nullptr, *d_dt = nullptr;
+  // solver
+  SolverArgs sa{};
+  double *d_Dinv64 = nullptr;
+  float* d_Dinv32 = nullptr;
+  double* d_norms = nullptr;
+  int *d_its = nullptr, *d_refs = nullptr, *d_status = nullptr;
+  double* d_relres = nullptr;
+  std::vector<eb_sim_stats> stats;
+  std::vector<double> h_norms;
+};
+
+namespace {
+
+__global__ void k_scatter(const int64_t* idx, const double* vals, int64_t n, double* dst) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[idx[t]] = vals[t];
+}
+
+int upload_mask(eb_handle* h, int* dst, const int32_t* mask) {
+  std::vector<int> m(h->n_sims, 1);
+  if (mask)
+    for (int s = 0; s < h->n_sims; ++s) m[s] = mask[s] != 0;
+  CK(cudaMemcpyAsync(dst, m.data(), sizeof(int) * h->n_sims, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return EB_OK;
+}
+
+int solve(eb_handle* h) {
+  launch_block_jacobi(h->d, h->d_Dinv64, h->d_Dinv32, h->stream);
+  CK(cudaGetLastError());
+  const bool fp32 = h->P.precision == EB_PREC_MIXED;
+  int threads = h->P.threads_per_sim > 0 ? h->P.threads_per_sim : 256;
+  CK(launch_gmres(h->sa, fp32, threads, h->stream));
+  return EB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* eb_last_error(void) { return g_err; }
+
+int eb_default_params(eb_params* p) {
+  if (!p) return fail(EB_ERR_ARG, "eb_default_params: null");
+  std::memset(p, 0, sizeof(*p));
+  p->alpha = -0.05;
+  p->beta = 0.25 * (1 - p->alpha) * (1 - p->alpha);
+  p->gamma = 0.5 * (1 - 2 * p->alpha);
+  p->tolerance_residual = 1e-5;
+  p->tolerance_displacement = 1e-5;
+  p->max_iterations = 20;
+  p->gauss_w[0] = 5.0 / 9.0; p->gauss_w[1] = 8.0 / 9.0; p->gauss_w[2] = 5.0 / 9.0;
+  p->gauss_z[0] = -std::sqrt(3.0 / 5.0); p->gauss_z[1] = 0.0; p->gauss_z[2] = std::sqrt(3.0 / 5.0);
+  p->precision = EB_PREC_FP64;
+  p->krylov_restart = 64;
+  p->krylov_max_iter = 4000;
+  p->linear_tol = 1e-10;
+  p->inner_tol = 1e-4;
+  p->max_refinements = 60;
+  p->threads_per_sim = 0;
+  return EB_OK;
+}
+
+int eb_device_info(int32_t* count, char* name, int32_t name_len) {
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (count) *count = (e == cudaSuccess) ? c : 0;
+  if (e != cudaSuccess) return fail(EB_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+  if (name && name_len > 0) {
+    cudaDeviceProp pr;
+    if (c > 0 && cudaGetDeviceProperties(&pr, 0) == cudaSuccess) {
+      std::snprintf(name, name_len, "%s (sm_%d%d, %d SMs)", pr.name, pr.major, pr.minor, pr.multiProcessorCount);
+    } else {
+      name[0] = 0;
+    }
+  }
+  return EB_OK;
+}
+
+int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_handle** out) {
+  if (!p || !sims || !out || n_sims <= 0) return fail(EB_ERR_ARG, "eb_create: bad arguments");
+  *out = nullptr;
+  if (p->krylov_restart < 1 || p->krylov_restart > 128) return fail(EB_ERR_ARG, "krylov_restart must be in [1,128]");
+  std::unique_ptr<eb_handle> h(new eb_handle());
+  h->P = *p;
+  h->n_sims = n_sims;
+  for (int i = 0; i < 3; ++i) { h->gauss.w[i] = p->gauss_w[i]; h->gauss.z[i] = p->gauss_z[i]; }
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+
+  // ---- sizes and offsets
+  h->node_off.assign(n_sims + 1, 0);
+  h->elem_off.assign(n_sims + 1, 0);
+  for (int s = 0; s < n_sims; ++s) {
+    const eb_sim_desc& S = sims[s];
+    if (S.n_nodes <= 0 || S.n_elem <= 0 || !S.X0 || !S.conn || !S.E || !S.nu || !S.rho || !S.radius || !S.damping)
+      return fail(EB_ERR_ARG, "sim %d: missing nodes, connectivity or material arrays", s);
+    for (int64_t e = 0; e < S.n_elem; ++e) {
+      int64_t a = S.conn[2 * e], b = S.conn[2 * e + 1];
+      if (a < 0 || b < 0 || a >= S.n_nodes || b >= S.n_nodes || a == b)
+        return fail(EB_ERR_ARG, "sim %d: element %lld has invalid nodes (%lld, %lld)", s, (long long)e, (long long)a,
+                    (long long)b);
+    }
+    for (int64_t k = 0; k < S.n_fixed; ++k)
+      if (S.fixed_dofs[k] < 0 || S.fixed_dofs[k] >= 6 * S.n_nodes) return fail(EB_ERR_ARG, "sim %d: fixed dof out of range", s);
+    for (int64_t k = 0; k < S.n_loaded; ++k)
+      if (S.loaded_dofs[k] < 0 || S.loaded_dofs[k] >= 6 * S.n_nodes) return fail(EB_ERR_ARG, "sim %d: loaded dof out of range", s);
+    if (S.surface == EB_SURFACE_SDF) {
+      if (!S.sdf_values || S.sdf_dims[0] < 1 || S.sdf_dims[1] < 1 || S.sdf_dims[2] < 1)
+        return fail(EB_ERR_ARG, "sim %d: SDF grid missing", s);
+      if (S.sdf_spacing[0] <= 0 || S.sdf_spacing[1] <= 0 || S.sdf_spacing[2] <= 0)
+        return fail(EB_ERR_ARG, "sim %d: SDF spacing must be positive", s);
+    }
+    h->node_off[s + 1] = h->node_off[s] + S.n_nodes;
+    h->elem_off[s + 1] = h->elem_off[s] + S.n_elem;
+  }
+  const int64_t NN = h->node_off[n_sims], NE = h->elem_off[n_sims], ND = 6 * NN;
+  if (NN >= (1LL << 31) / 6 || NE >= (1LL << 29)) return fail(EB_ERR_ARG, "problem too large for 32-bit indices");
+
+  // ---- host staging of node and element data
+  std::vector<double> X0(3 * NN), u(3 * NN), ud(3 * NN), udd(3 * NN), w(3 * NN), wd(3 * NN), wdd(3 * NN);
+  std::vector<double> R(9 * NN), dR(9 * NN, 0.0);
+  std::vector<int> node_sim(NN);
+  std::vector<int> ea(NE), ebv(NE), elem_sim(NE);
+  std::vector<double> l0(NE), Re0(9 * NE), Kbar(7 * NE), Jr(3 * NE), Ar(NE), damp(NE), radius(NE);
+  std::vector<uint8_t> is_contact(NE, 0);
+  std::vector<uint8_t> fixed(ND, 0);
+  std::vector<double> fext(ND, 0.0);
+  h->has_contact.assign(n_sims, 0);
+  std::vector<int> has_fixed(n_sims, 0);
+  std::vector<SurfaceDev> surf(n_sims);
+  std::vector<ContactProps> props(n_sims);
+  std::vector<std::vector<double>> sdf_coefs(n_sims);
+  h->load_off.assign(n_sims + 1, 0);
+  h->fix_off.assign(n_sims + 1, 0);
+
+  for (int s = 0; s < n_sims; ++s) {
+    const eb_sim_desc& S = sims[s];
+    const int64_t no = h->node_off[s], eo = h->elem_off[s];
+    auto put3 = [&](std::vector<double>& dst, const double* src) {
+      for (int64_t i = 0; i < S.n_nodes; ++i)
+        for (int k = 0; k < 3; ++k) dst[k * NN + no + i] = src ? src[3 * i + k] : 0.0;
+    };
+    put3(X0, S.X0); put3(u, S.u); put3(ud, S.ud); put3(udd, S.udd); put3(w, S.w); put3(wd, S.wd); put3(wdd, S.wdd);
+    for (int64_t i = 0; i < S.n_nodes; ++i) {
+      node_sim[no + i] = s;
+      for (int k = 0; k < 9; ++k) {
+        R[k * NN + no + i] = S.R ? S.R[9 * i + k] : ((k % 4 == 0) ? 1.0 : 0.0);
+        dR[k * NN + no + i] = (k % 4 == 0) ? 1.0 : 0.0;
+      }
+    }
+    for (int64_t e = 0; e < S.n_elem; ++e) {
+      const int64_t ge = eo + e;
+      const int64_t a = S.conn[2 * e], b = S.conn[2 * e + 1];
+      ea[ge] = (int)(no + a);
+      ebv[ge] = (int)(no + b);
+      elem_sim[ge] = s;
+      const double* Xa = S.X0 + 3 * a;
+      const double* Xb = S.X0 + 3 * b;
+      const double dx = Xa[0] - Xb[0], dy = Xa[1] - Xb[1], dz = Xa[2] - Xb[2];
+      const double L = std::sqrt(dx * dx + dy * dy + dz * dz);  // def_beam.jl:136
+      l0[ge] = L;
+      double Rm[9];
+      if (S.Re0) std::memcpy(Rm, S.Re0 + 9 * e, sizeof(Rm));
+      else initial_frame(Xa, Xb, Rm);
+      for (int k = 0; k < 9; ++k) Re0[k * NE + ge] = Rm[k];
+      // BeamMaterialProperties / K̄ⁱⁿᵗ_beam (def_beam.jl:144-155, 205-219)
+      const double E = S.E[e], nu = S.nu[e], rho = S.rho[e], r = S.radius[e];
+      const double G = E / (2 * (1 + nu));
+      const double A = M_PI * r * r;
+      const double I22 = M_PI * std::pow(r, 4) / 4, I33 = I22, Io = I22 + I33;
+      const double kb[7] = {A * E / L,     G * Io / L,        4 * E * I33 / L, 4 * E * I22 / L,
+                            -G * Io / L,   2 * E * I33 / L,   2 * E * I22 / L};
+      for (int k = 0; k < 7; ++k) Kbar[k * NE + ge] = kb[k];
+      Jr[ge] = rho * Io; Jr[NE + ge] = rho * I22; Jr[2 * NE + ge] = rho * I33;
+      Ar[ge] = rho * A;
+      damp[ge] = S.damping[e];
+      radius[ge] = r;
+    }
+    // contact
+    if (S.surface != EB_SURFACE_NONE) {
+      h->has_contact[s] = 1;
+      h->any_contact = true;
+      if (S.contact_elems && S.n_contact_elems > 0) {
+        for (int64_t c = 0; c < S.n_contact_elems; ++c) {
+          int64_t e = S.contact_elems[c];
+          if (e < 0 || e >= S.n_elem) return fail(EB_ERR_ARG, "sim %d: contact element out of range", s);
+          is_contact[eo + e] = 1;
+        }
+      } else {
+        for (int64_t e = 0; e < S.n_elem; ++e) is_contact[eo + e] = 1;
+      }
+      props[s] = ContactProps{S.kn, S.mu, S.eps_t, S.eta_n};
+      SurfaceDev& sf = surf[s];
+      std::memset(&sf, 0, sizeof(sf));
+      if (S.surface == EB_SURFACE_SPHERE) {
+        sf.kind = 0;
+        sf.cx = S.sphere_center[0]; sf.cy = S.sphere_center[1]; sf.cz = S.sphere_center[2];
+        sf.R = S.sphere_radius;
+      } else {
+        sf.kind = 1;
+        sf.nx = (int)S.sdf_dims[0]; sf.ny = (int)S.sdf_dims[1]; sf.nz = (int)S.sdf_dims[2];
+        sf.x0 = S.sdf_origin[0]; sf.y0 = S.sdf_origin[1]; sf.z0 = S.sdf_origin[2];
+        sf.ihx = 1.0 / S.sdf_spacing[0]; sf.ihy = 1.0 / S.sdf_spacing[1]; sf.ihz = 1.0 / S.sdf_spacing[2];
+        sf.xl = (double)(sf.nx - 1) * S.sdf_spacing[0];
+        sf.yl = (double)(sf.ny - 1) * S.sdf_spacing[1];
+        sf.zl = (double)(sf.nz - 1) * S.sdf_spacing[2];
+        sdf_coefs[s] = sdf_coefficients(S.sdf_values, S.sdf_dims, S.sdf_inside == 0);
+      }
+    }
+    // BCs and loads
+    for (int64_t k = 0; k < S.n_fixed; ++k) {
+      fixed[6 * no + S.fixed_dofs[k]] = 1;
+      h->fix_dof.push_back(6 * no + S.fixed_dofs[k]);
+    }
+    has_fixed[s] = S.n_fixed > 0;
+    for (int64_t k = 0; k < S.n_loaded; ++k) {
+      h->load_dof.push_back(6 * no + S.loaded_dofs[k]);
+      fext[6 * no + S.loaded_dofs[k]] = S.fext0 ? S.fext0[k] : 0.0;  // Forces(conf), def_structures.jl:155-167
+    }
+    h->fix_off[s + 1] = h->fix_off[s] + S.n_fixed;
+    h->load_off[s + 1] = h->load_off[s] + S.n_loaded;
+  }
+
+  // ---- block pattern: union of the elements' node pairs (sparse_matrices.jl:6-77, in 6x6 blocks)
+  std::vector<std::vector<int>> adj(NN);
+  for (int64_t i = 0; i < NN; ++i) adj[i].push_back((int)i);
+  for (int64_t e = 0; e < NE; ++e) {
+    adj[ea[e]].push_back(ebv[e]);
+    adj[ebv[e]].push_back(ea[e]);
+  }
+  std::vector<int> row_ptr(NN + 1, 0), col, diag_blk(NN), blk_sim;
+  for (int64_t i = 0; i < NN; ++i) {
+    auto& v = adj[i];
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    row_ptr[i + 1] = row_ptr[i] + (int)v.size();
+    for (int c : v) {
+      if (c == (int)i) diag_blk[i] = (int)col.size();
+      col.push_back(c);
+      blk_sim.push_back(node_sim[i]);
+    }
+  }
+  const int64_t NB = (int64_t)col.size();
+  auto blk_of = [&](int r, int c) {
+    auto b = std::lower_bound(col.begin() + row_ptr[r], col.begin() + row_ptr[r + 1], c);
+    return (int)(b - col.begin());
+  };
+  // ordered contribution lists (element order) per block and per node
+  std::vector<int> bcnt(NB + 1, 0), ncnt(NN + 1, 0);
+  for (int64_t e = 0; e < NE; ++e) {
+    const int nd[2] = {ea[e], ebv[e]};
+    for (int J = 0; J < 2; ++J)
+      for (int I = 0; I < 2; ++I) bcnt[blk_of(nd[I], nd[J]) + 1]++;
+    ncnt[nd[0] + 1]++;
+    ncnt[nd[1] + 1]++;
+  }
+  for (int64_t b = 0; b < NB; ++b) bcnt[b + 1] += bcnt[b];
+  for (int64_t i = 0; i < NN; ++i) ncnt[i + 1] += ncnt[i];
+  std::vector<int> blk_contrib(bcnt[NB]), node_contrib(ncnt[NN]);
+  {
+    std::vector<int> bf(bcnt.begin(), bcnt.end() - 1), nf(ncnt.begin(), ncnt.end() - 1);
+    for (int64_t e = 0; e < NE; ++e) {
+      const int nd[2] = {ea[e], ebv[e]};
+      for (int J = 0; J < 2; ++J)
+        for (int I = 0; I < 2; ++I) blk_contrib[bf[blk_of(nd[I], nd[J])]++] = (int)(4 * e + I + 2 * J);
+      node_contrib[nf[nd[0]]++] = (int)(2 * e);
+      node_contrib[nf[nd[1]]++] = (int)(2 * e + 1);
+    }
+  }
+  h->blk_off.assign(n_sims + 1, 0);
+  for (int s = 0; s < n_sims; ++s) h->blk_off[s + 1] = row_ptr[h->node_off[s + 1]];
+
+  // ---- device arenas
+  Arena& A = h->arena;
+  Dev& d = h->d;
+  d.n_sims = n_sims;
+  d.n_nodes = NN;
+  d.n_elem = NE;
+  d.nnzb = NB;
+  d.n_dof = ND;
+  int64_t *p_node_off, *p_blk_off;
+  CK(A.upload(&p_node_off, h->node_off));
+  CK(A.upload(&p_blk_off, h->blk_off));
+  d.sim_node_off = p_node_off;
+  d.sim_blk_off = p_blk_off;
+  CK(A.alloc(&h->d_active, n_sims));
+  CK(A.alloc(&h->d_mask, n_sims));
+  CK(A.alloc(&h->d_cK, n_sims));
+  CK(A.alloc(&h->d_cC, n_sims));
+  CK(A.alloc(&h->d_cM, n_sims));
+  CK(A.alloc(&h->d_dt, n_sims));
+  d.active = h->d_active; d.cK = h->d_cK; d.cC = h->d_cC; d.cM = h->d_cM; d.dt = h->d_dt;
+  // SDF coefficient grids
+  for (int s = 0; s < n_sims; ++s)
+    if (!sdf_coefs[s].empty()) {
+      double* c;
+      CK(A.upload(&c, sdf_coefs[s]));
+      surf[s].coef = c;
+    }
+  SurfaceDev* p_surf;
+  ContactProps* p_props;
+  int* p_hf;
+  CK(A.upload(&p_surf, surf));
+  CK(A.upload(&p_props, props));
+  CK(A.upload(&p_hf, has_fixed));
+  d.surf = p_surf; d.props = p_props; d.has_fixed = p_hf;
+  int* p_ns;
+  CK(A.upload(&p_ns, node_sim));
+  d.node_sim = p_ns;
+  double* pX0;
+  CK(A.upload(&pX0, X0));
+  d.X0 = pX0;
+  CK(A.upload(&d.u, u)); CK(A.upload(&d.ud, ud)); CK(A.upload(&d.udd, udd));
+  CK(A.upload(&d.w, w)); CK(A.upload(&d.wd, wd)); CK(A.upload(&d.wdd, wdd));
+  CK(A.upload(&d.R, R)); CK(A.upload(&d.dR, dR));
+  CK(A.upload(&d.un, u)); CK(A.upload(&d.udn, ud)); CK(A.upload(&d.uddn, udd));
+  CK(A.upload(&d.wn, w)); CK(A.upload(&d.wdn, wd)); CK(A.upload(&d.wddn, wdd));
+  CK(A.upload(&d.Rn, R)); CK(A.upload(&d.dRn, dR));
+  int *p_ea, *p_eb, *p_es;
+  CK(A.upload(&p_ea, ea)); CK(A.upload(&p_eb, ebv)); CK(A.upload(&p_es, elem_sim));
+  d.ea = p_ea; d.eb = p_eb; d.elem_sim = p_es;
+  double *p_l0, *p_Re0, *p_Kb, *p_Jr, *p_Ar, *p_dm, *p_rd;
+  CK(A.upload(&p_l0, l0)); CK(A.upload(&p_Re0, Re0)); CK(A.upload(&p_Kb, Kbar)); CK(A.upload(&p_Jr, Jr));
+  CK(A.upload(&p_Ar, Ar)); CK(A.upload(&p_dm, damp)); CK(A.upload(&p_rd, radius));
+  d.l0 = p_l0; d.Re0 = p_Re0; d.Kbar = p_Kb; d.Jr = p_Jr; d.Ar = p_Ar; d.damp = p_dm; d.radius = p_rd;
+  uint8_t* p_ic;
+  CK(A.upload(&p_ic, is_contact));
+  d.is_contact = p_ic;
+  CK(A.alloc(&d.stK, NE * 144)); CK(A.alloc(&d.stC, NE * 144)); CK(A.alloc(&d.stM, NE * 144));
+  CK(A.alloc(&d.stTi, NE * 12)); CK(A.alloc(&d.stTk, NE * 12)); CK(A.alloc(&d.stE, NE * 2));
+  if (h->any_contact) {
+    CK(A.alloc(&d.scK, NE * 144)); CK(A.alloc(&d.scC, NE * 144)); CK(A.alloc(&d.scT, NE * 12));
+    CK(A.alloc(&d.scE, NE));
+  }
+  CK(A.alloc(&d.sc_on, NE));
+  int *p_rp, *p_col, *p_db, *p_bs, *p_bc, *p_bcl, *p_nc, *p_ncl;
+  CK(A.upload(&p_rp, row_ptr)); CK(A.upload(&p_col, col)); CK(A.upload(&p_db, diag_blk)); CK(A.upload(&p_bs, blk_sim));
+  CK(A.upload(&p_bc, bcnt)); CK(A.upload(&p_bcl, blk_contrib)); CK(A.upload(&p_nc, ncnt)); CK(A.upload(&p_ncl, node_contrib));
+  d.row_ptr = p_rp; d.col = p_col; d.diag_blk = p_db; d.blk_sim = p_bs; d.blk_cptr = p_bc; d.blk_contrib = p_bcl;
+  d.node_cptr = p_nc; d.node_contrib = p_ncl;
+  CK(A.alloc(&d.K1, NB * 36)); CK(A.alloc(&d.C1, NB * 36)); CK(A.alloc(&d.M1, NB * 36));
+  CK(A.alloc(&d.Kn, NB * 36)); CK(A.alloc(&d.Cn, NB * 36)); CK(A.alloc(&d.Mn, NB * 36));
+  CK(A.alloc(&d.Kt, NB * 36)); CK(A.alloc(&d.Kt32, NB * 36));
+  CK(A.alloc(&d.D, ND)); CK(A.alloc(&d.Dd, ND)); CK(A.alloc(&d.Ddd, ND)); CK(A.alloc(&d.dD, ND)); CK(A.alloc(&d.r, ND));
+  CK(A.upload(&d.fext1, fext)); CK(A.upload(&d.fextn, fext));
+  CK(A.alloc(&d.Ti1, ND)); CK(A.alloc(&d.Tin, ND)); CK(A.alloc(&d.Tk1, ND)); CK(A.alloc(&d.Tkn, ND));
+  CK(A.alloc(&d.Tc1, ND)); CK(A.alloc(&d.Tcn, ND));
+  CK(A.upload(&d.fixed, fixed));
+  CK(A.alloc(&d.imposed, ND));
+  CK(A.upload(&h->d_load_dof, h->load_dof));
+  CK(A.upload(&h->d_fix_dof, h->fix_dof));
+  CK(A.alloc(&h->d_vals, std::max<size_t>(h->load_dof.size(), h->fix_dof.size()) + 1));
+
+  // ---- solver work
+  const int m = p->krylov_restart;
+  const bool fp32 = p->precision == EB_PREC_MIXED;
+  CK(A.alloc(&h->d_Dinv64, NN * 36));
+  CK(A.alloc(&h->d_Dinv32, NN * 36));
+  CK(A.alloc(&h->d_norms, 4 * (size_t)n_sims));
+  CK(A.alloc(&h->d_its, n_sims)); CK(A.alloc(&h->d_refs, n_sims)); CK(A.alloc(&h->d_status, n_sims));
+  CK(A.alloc(&h->d_relres, n_sims));
+  SolverArgs& sa = h->sa;
+  sa.n_sims = n_sims;
+  sa.sim_node_off = d.sim_node_off;
+  sa.active = d.active;
+  sa.row_ptr = d.row_ptr;
+  sa.col = d.col;
+  sa.Kt = d.Kt;
+  sa.Kt32 = d.Kt32;
+  sa.Dinv64 = h->d_Dinv64;
+  sa.Dinv32 = h->d_Dinv32;
+  sa.fixed = d.fixed;
+  sa.b = d.r;
+  sa.dD = d.dD;
+  sa.fext1 = d.fext1;
+  sa.Tc1 = d.Tc1;
+  sa.Tk1 = d.Tk1;
+  CK(A.alloc(&sa.X, ND));
+  CK(A.alloc(&sa.R64, ND));
+  if (fp32) {
+    float *V, *Z;
+    CK(A.alloc(&V, (size_t)(m + 1) * ND)); CK(A.alloc(&Z, ND));
+    sa.V = V; sa.Z = Z;
+  } else {
+    double *V, *Z;
+    CK(A.alloc(&V, (size_t)(m + 1) * ND)); CK(A.alloc(&Z, ND));
+    sa.V = V; sa.Z = Z;
+  }
+  sa.m = m;
+  sa.max_iter = p->krylov_max_iter;
+  sa.max_ref = p->max_refinements;
+  sa.tol = p->linear_tol;
+  sa.inner_tol = fp32 ? p->inner_tol : p->linear_tol;
+  sa.norms = h->d_norms;
+  sa.its = h->d_its;
+  sa.refs = h->d_refs;
+  sa.relres = h->d_relres;
+  sa.status = h->d_status;
+  h->stats.assign(n_sims, eb_sim_stats{});
+  h->h_norms.assign(4 * (size_t)n_sims, 0.0);
+
+  // ---- initialize_state_simulation! (inizialization.jl:37-44): beams only, matricesⁿ ← matricesⁿ⁺¹
+  int rc = upload_mask(h.get(), h->d_active, nullptr);
+  if (rc) return rc;
+  launch_beam(d, h->gauss, h->stream);
+  launch_gather(d, p->alpha, false, h->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(d.Kn, d.K1, sizeof(double) * NB * 36, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(d.Cn, d.C1, sizeof(double) * NB * 36, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(d.Mn, d.M1, sizeof(double) * NB * 36, cudaMemcpyDeviceToDevice, h->stream));
+  // forcesⁿ (Tⁱⁿᵗ, Tᵏ, Tᶜ) stay zero after this call, as in the reference
+  CK(cudaStreamSynchronize(h->stream));
+  *out = h.release();
+  return EB_OK;
+}
+
+int eb_destroy(eb_handle* h) {
+  if (!h) return EB_OK;
+  if (h->stream) {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+  }
+  delete h;
+  return EB_OK;
+}
+
+static int set_values(eb_handle* h, int32_t sim, const double* values, const std::vector<int64_t>& off,
+                      const int64_t* d_idx, double* dst) {
+  if (!h || sim < 0 || sim >= h->n_sims) return fail(EB_ERR_ARG, "bad handle or sim index");
+  const int64_t o = off[sim], n = off[sim + 1] - o;
+  if (n == 0) return EB_OK;
+  if (!values) return fail(EB_ERR_ARG, "values is null");
+  CK(cudaMemcpyAsync(h->d_vals, values, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  k_scatter<<<nblocks(n, 256), 256, 0, h->stream>>>(d_idx + o, h->d_vals, n, dst);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return EB_OK;
+}
+
+int eb_set_loads(eb_handle* h, int32_t sim, const double* values) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  return set_values(h, sim, values, h->load_off, h->d_load_dof, h->d.fext1);
+}
+
+int eb_set_imposed(eb_handle* h, int32_t sim, const double* values) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  return set_values(h, sim, values, h->fix_off, h->d_fix_dof, h->d.imposed);
+}
+
+int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_out, int32_t* status_out) {
+  if (!h || !dt || !k_out) return fail(EB_ERR_ARG, "eb_step: bad arguments");
+  const int S = h->n_sims;
+  const eb_params& P = h->P;
+  const double a = P.alpha, b = P.beta, g = P.gamma;
+  std::vector<double> cK(S), cC(S), cM(S), dts(S);
+  std::vector<int> act(S), iter(S, 0), k(S, 1);
+  for (int s = 0; s < S; ++s) {
+    act[s] = active ? (active[s] != 0) : 1;
+    if (act[s] && !(dt[s] > 0)) return fail(EB_ERR_ARG, "eb_step: dt[%d] must be positive", s);
+    dts[s] = dt[s];
+    cK[s] = 1 + a;
+    cC[s] = g / (b * dt[s]);
+    cM[s] = 1 / (b * (dt[s] * dt[s]));
+  }
+  cudaStream_t st = h->stream;
+  CK(cudaMemcpyAsync(h->d_cK, cK.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->d_cC, cC.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->d_cM, cM.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->d_dt, dts.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->d_active, act.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(h->d_its, 0, sizeof(int) * S, st));
+  CK(cudaMemsetAsync(h->d_refs, 0, sizeof(int) * S, st));
+  CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * S, st));
+  CK(cudaMemsetAsync(h->d_relres, 0, sizeof(double) * S, st));
+  const Dev& d = h->d;
+
+  // ---- predictor! (predictor.jl:1-27)
+  launch_init_predictor(d, st);
+  launch_predictor_rhs(d, a, b, g, st);
+  launch_apply_bc(d, st);
+  int rc = solve(h);
+  if (rc) return rc;
+  launch_global_predictor(d, b, g, st);
+  launch_local_predictor(d, b, g, st);
+
+  // ---- corrector! (corrector.jl:1-59)
+  launch_init_corrector(d, st);
+  CK(cudaGetLastError());
+  std::vector<double> res(S, INFINITY), dn(S, INFINITY);
+  std::vector<int> running(S);
+  for (int s = 0; s < S; ++s) running[s] = act[s] && (1 <= P.max_iterations);
+  while (true) {
+    bool any = false;
+    for (int s = 0; s < S; ++s) any |= running[s] != 0;
+    if (!any) break;
+    CK(cudaMemcpyAsync(h->d_active, running.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    launch_beam(d, h->gauss, st);
+    if (h->any_contact) launch_contact(d, h->gauss, st);
+    launch_gather(d, a, h->any_contact, st);
+    launch_corrector_rhs(d, a, st);
+    launch_apply_bc(d, st);
+    rc = solve(h);
+    if (rc) return rc;
+    launch_global_corrector(d, st);
+    launch_local_corrector(d, b, g, st);
+    CK(cudaMemcpyAsync(h->h_norms.data(), h->d_norms, sizeof(double) * 4 * S, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int s = 0; s < S; ++s) {
+      if (!running[s]) continue;
+      const double* q = &h->h_norms[4 * s];
+      // compute_norms_corrector (utils_solver.jl:126-151)
+      double dnorm = std::sqrt(q[0]);
+      double rn = std::sqrt(q[1]);
+      const double fn = std::sqrt(q[2]), en = std::sqrt(q[3]);
+      if (fn + en > 1e-12) rn = rn / (fn + en);
+      res[s] = rn;
+      dn[s] = dnorm;
+      ++iter[s];
+      k[s] += 1;
+      running[s] = (res[s] > P.tolerance_residual || dn[s] > P.tolerance_displacement) && k[s] <= P.max_iterations;
+    }
+  }
+  // ---- statistics
+  std::vector<int> its(S), refs(S), status(S);
+  std::vector<double> rel(S);
+  CK(cudaMemcpyAsync(its.data(), h->d_its, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(refs.data(), h->d_refs, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(status.data(), h->d_status, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(rel.data(), h->d_relres, sizeof(double) * S, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int s = 0; s < S; ++s) {
+    eb_sim_stats& q = h->stats[s];
+    if (!act[s]) continue;
+    int stt = status[s];
+    if (!std::isfinite(res[s]) || !std::isfinite(dn[s])) stt = EB_SIM_NAN;
+    if (k[s] > P.max_iterations && stt == EB_SIM_OK) stt = EB_SIM_NOT_CONVERGED;
+    q.newton_iterations = iter[s];
+    q.krylov_iterations = its[s];
+    q.refinements = refs[s];
+    q.status = stt;
+    q.last_res_norm = res[s];
+    q.last_dD_norm = dn[s];
+    q.max_linear_rel_residual = rel[s];
+    k_out[s] = k[s];
+    if (status_out) status_out[s] = stt;
+  }
+  return EB_OK;
+}
+
+static int commit_impl(eb_handle* h, const int32_t* mask, bool commit) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  int rc = upload_mask(h, h->d_mask, mask);
+  if (rc) return rc;
+  launch_commit(h->d, h->d_mask, commit, h->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return EB_OK;
+}
+
+int eb_commit(eb_handle* h, const int32_t* mask) { return commit_impl(h, mask, true); }
+int eb_rollback(eb_handle* h, const int32_t* mask) { return commit_impl(h, mask, false); }
+
+static int get_state_impl(eb_handle* h, int32_t sim, bool at_n, double* u, double* ud, double* udd, double* w,
+                          double* wd, double* wdd, double* R, double* dR) {
+  if (!h || sim < 0 || sim >= h->n_sims) return fail(EB_ERR_ARG, "bad handle or sim index");
+  const int64_t NN = h->d.n_nodes, o = h->node_off[sim], n = h->node_off[sim + 1] - o;
+  const Dev& d = h->d;
+  double* src[8] = {at_n ? d.un : d.u,   at_n ? d.udn : d.ud, at_n ? d.uddn : d.udd, at_n ? d.wn : d.w,
+                    at_n ? d.wdn : d.wd, at_n ? d.wddn : d.wdd, at_n ? d.Rn : d.R,   at_n ? d.dRn : d.dR};
+  double* dst[8] = {u, ud, udd, w, wd, wdd, R, dR};
+  const int nc[8] = {3, 3, 3, 3, 3, 3, 9, 9};
+  std::vector<double> tmp((size_t)n);
+  for (int f = 0; f < 8; ++f) {
+    if (!dst[f]) continue;
+    for (int k = 0; k < nc[f]; ++k) {
+      CK(cudaMemcpy(tmp.data(), src[f] + k * NN + o, sizeof(double) * n, cudaMemcpyDeviceToHost));
+      for (int64_t i = 0; i < n; ++i) dst[f][nc[f] * i + k] = tmp[i];
+    }
+  }
+  return EB_OK;
+}
+
+int eb_get_state(eb_handle* h, int32_t sim, double* u, double* ud, double* udd, double* w, double* wd, double* wdd,
+                 double* R, double* dR) {
+  return get_state_impl(h, sim, false, u, ud, udd, w, wd, wdd, R, dR);
+}
+int eb_get_state_n(eb_handle* h, int32_t sim, double* u, double* ud, double* udd, double* w, double* wd,
+                   double* wdd, double* R, double* dR) {
+  return get_state_impl(h, sim, true, u, ud, udd, w, wd, wdd, R, dR);
+}
+
+int eb_get_stats(eb_handle* h, eb_sim_stats* stats) {
+  if (!h || !stats) return fail(EB_ERR_ARG, "bad arguments");
+  std::memcpy(stats, h->stats.data(), sizeof(eb_sim_stats) * h->n_sims);
+  return EB_OK;
+}
+
+int eb_get_forces(eb_handle* h, int32_t sim, double* Tint, double* Tk, double* Tc) {
+  if (!h || sim < 0 || sim >= h->n_sims) return fail(EB_ERR_ARG, "bad handle or sim index");
+  const int64_t o = 6 * h->node_off[sim], n = 6 * (h->node_off[sim + 1] - h->node_off[sim]);
+  if (Tint) CK(cudaMemcpy(Tint, h->d.Ti1 + o, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (Tk) CK(cudaMemcpy(Tk, h->d.Tk1 + o, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (Tc) CK(cudaMemcpy(Tc, h->d.Tc1 + o, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return EB_OK;
+}
+
+}  // extern "C"

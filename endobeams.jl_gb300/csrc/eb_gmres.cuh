@@ -1,0 +1,40 @@
+// Per-simulation GMRES solver interface (implementation in eb_gmres.cu).
+#pragma once
+#include "eb_internal.cuh"
+
+namespace eb {
+
+struct SolverArgs {
+  int n_sims;
+  const int64_t* sim_node_off;
+  const int* active;
+  const int* row_ptr;
+  const int* col;
+  const double* Kt;
+  const float* Kt32;
+  const double* Dinv64;
+  const float* Dinv32;
+  const uint8_t* fixed;
+  const double* b;       // right-hand side (Newton residual after the BC lift)
+  double* dD;            // free components receive the solution
+  const double* fext1;   // for the Newton norms
+  const double* Tc1;
+  const double* Tk1;
+  double* X;             // n_dof work
+  double* R64;           // n_dof work
+  void* V;               // (m+1) n_dof Krylov basis (double or float)
+  void* Z;               // n_dof work (double or float)
+  int m, max_iter, max_ref;
+  double tol, inner_tol;
+  double* norms;         // 4 per sim: |ΔD_free|², |r_free|², |f_free|², |f_fixed|²
+  int* its;              // per sim, accumulated
+  int* refs;             // per sim, accumulated
+  double* relres;        // per sim, max over the step
+  int* status;           // per sim, max over the step
+};
+
+void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream_t s);
+cudaError_t launch_gmres(const SolverArgs& a, bool fp32, int threads, cudaStream_t s);
+size_t gmres_smem(int m);
+
+}  // namespace eb

@@ -1,0 +1,136 @@
+// Element-level testing entry points: evaluate the device beam and contact
+// elements on caller-supplied packed states, so the kernels can be compared
+// with a CPU evaluation of compute_beams / compute_contact_beams for the
+// same inputs.
+//
+// Packed input record (96 doubles): X1[3] X2[3] u1[3] u2[3] R1[9] R2[9] ΔR1[9]
+// ΔR2[9] u̇1[3] u̇2[3] ẇ1[3] ẇ2[3] ü1[3] ü2[3] ẅ1[3] ẅ2[3] l0 Rₑ⁰[9] K̄ū K̄Θ[3]
+// K̄ΘΘ[3] Jᵨ[3] Aᵨ damping radius (pad).  3x3 matrices column-major.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/endobeams_gb300.h"
+#include "eb_contact.cuh"
+
+using namespace ebd;
+
+namespace {
+thread_local char g_err2[512];
+
+__device__ __forceinline__ V3 P3(const double* p) { return v3(p[0], p[1], p[2]); }
+__device__ __forceinline__ M3 P9(const double* p) {
+  M3 m;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) m.a[k] = p[k];
+  return m;
+}
+
+__global__ void k_element_eval(int64_t n, const double* in, Gauss3 g, double* out) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const double* p = in + 96 * e;
+  double* o = out + 458 * e;
+  BeamIn b;
+  b.X1 = P3(p + 0); b.X2 = P3(p + 3); b.u1 = P3(p + 6); b.u2 = P3(p + 9);
+  b.R1 = P9(p + 12); b.R2 = P9(p + 21); b.dR1 = P9(p + 30); b.dR2 = P9(p + 39);
+  b.ud1 = P3(p + 48); b.ud2 = P3(p + 51); b.wd1 = P3(p + 54); b.wd2 = P3(p + 57);
+  b.udd1 = P3(p + 60); b.udd2 = P3(p + 63); b.wdd1 = P3(p + 66); b.wdd2 = P3(p + 69);
+  b.l0 = p[72]; b.Re0 = P9(p + 73); b.Ku = p[82]; b.KT = P3(p + 83); b.KTT = P3(p + 86); b.Jr = P3(p + 89);
+  b.Ar = p[92]; b.damping = p[93];
+  BeamOut bo{o + 26, o + 170, o + 314, o + 2, o + 14, o + 0};
+  beam_element(b, g, bo);
+}
+
+__global__ void k_contact_eval(int64_t n, const double* in, Gauss3 g, ContactProps cp, SurfaceDev s, double* out,
+                               int32_t* flags) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const double* p = in + 96 * e;
+  double* o = out + 301 * e;
+  ContactIn c;
+  c.X1 = P3(p + 0); c.X2 = P3(p + 3); c.u1 = P3(p + 6); c.u2 = P3(p + 9);
+  c.R1 = P9(p + 12); c.R2 = P9(p + 21); c.dR1 = P9(p + 30); c.dR2 = P9(p + 39);
+  c.ud1 = P3(p + 48); c.ud2 = P3(p + 51); c.wd1 = P3(p + 54); c.wd2 = P3(p + 57);
+  c.l0 = p[72]; c.Re0 = P9(p + 73); c.radius = p[94];
+  ContactOut co{o + 13, o + 157, o + 1, o + 0};
+  bool any = false;
+  contact_element(c, g, cp, s, co, &any);
+  flags[e] = any ? 1 : 0;
+}
+
+struct DBuf {
+  void* p = nullptr;
+  ~DBuf() { if (p) cudaFree(p); }
+};
+
+}  // namespace
+
+// defined in eb_abi.cu
+std::vector<double> eb_sdf_coefficients_host(const double* values, const int64_t dims[3], bool negate);
+int eb_internal_fail(int code, const char* msg);
+
+namespace {
+int err(const char* what, cudaError_t e) {
+  std::snprintf(g_err2, sizeof(g_err2), "%s: %s", what, cudaGetErrorString(e));
+  return eb_internal_fail(EB_ERR_CUDA, g_err2);
+}
+}  // namespace
+
+extern "C" int eb_element_eval(int64_t n, const double* in, const double* gauss6, double* out) {
+  if (n <= 0 || !in || !gauss6 || !out) return EB_ERR_ARG;
+  Gauss3 g;
+  for (int i = 0; i < 3; ++i) { g.w[i] = gauss6[i]; g.z[i] = gauss6[3 + i]; }
+  DBuf di, dout;
+  cudaError_t e;
+  if ((e = cudaMalloc(&di.p, sizeof(double) * 96 * n)) != cudaSuccess) return err("cudaMalloc", e);
+  if ((e = cudaMalloc(&dout.p, sizeof(double) * 458 * n)) != cudaSuccess) return err("cudaMalloc", e);
+  cudaMemcpy(di.p, in, sizeof(double) * 96 * n, cudaMemcpyHostToDevice);
+  cudaMemset(dout.p, 0, sizeof(double) * 458 * n);
+  k_element_eval<<<(unsigned)((n + 127) / 128), 128>>>(n, (const double*)di.p, g, (double*)dout.p);
+  if ((e = cudaGetLastError()) != cudaSuccess) return err("k_element_eval launch", e);
+  if ((e = cudaMemcpy(out, dout.p, sizeof(double) * 458 * n, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return err("k_element_eval", e);
+  return EB_OK;
+}
+
+extern "C" int eb_contact_eval(int64_t n, const double* in, const double* gauss6, const double* props,
+                               const double* surf, const double* values, double* out, int32_t* flags) {
+  if (n <= 0 || !in || !gauss6 || !props || !surf || !out || !flags) return EB_ERR_ARG;
+  Gauss3 g;
+  for (int i = 0; i < 3; ++i) { g.w[i] = gauss6[i]; g.z[i] = gauss6[3 + i]; }
+  ContactProps cp{props[0], props[1], props[2], props[3]};
+  SurfaceDev s;
+  std::memset(&s, 0, sizeof(s));
+  s.kind = (int)surf[0];
+  s.cx = surf[1]; s.cy = surf[2]; s.cz = surf[3]; s.R = surf[4];
+  DBuf dcoef, di, dout, dfl;
+  cudaError_t e;
+  if (s.kind == 1) {
+    if (!values) return EB_ERR_ARG;
+    int64_t dims[3] = {(int64_t)surf[5], (int64_t)surf[6], (int64_t)surf[7]};
+    std::vector<double> c = eb_sdf_coefficients_host(values, dims, false);
+    if ((e = cudaMalloc(&dcoef.p, sizeof(double) * c.size())) != cudaSuccess) return err("cudaMalloc", e);
+    cudaMemcpy(dcoef.p, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice);
+    s.coef = (const double*)dcoef.p;
+    s.nx = (int)dims[0]; s.ny = (int)dims[1]; s.nz = (int)dims[2];
+    s.x0 = surf[8]; s.y0 = surf[9]; s.z0 = surf[10];
+    s.ihx = 1.0 / surf[11]; s.ihy = 1.0 / surf[12]; s.ihz = 1.0 / surf[13];
+    s.xl = (s.nx - 1) * surf[11]; s.yl = (s.ny - 1) * surf[12]; s.zl = (s.nz - 1) * surf[13];
+  }
+  if ((e = cudaMalloc(&di.p, sizeof(double) * 96 * n)) != cudaSuccess) return err("cudaMalloc", e);
+  if ((e = cudaMalloc(&dout.p, sizeof(double) * 301 * n)) != cudaSuccess) return err("cudaMalloc", e);
+  if ((e = cudaMalloc(&dfl.p, sizeof(int32_t) * n)) != cudaSuccess) return err("cudaMalloc", e);
+  cudaMemcpy(di.p, in, sizeof(double) * 96 * n, cudaMemcpyHostToDevice);
+  cudaMemset(dout.p, 0, sizeof(double) * 301 * n);
+  k_contact_eval<<<(unsigned)((n + 127) / 128), 128>>>(n, (const double*)di.p, g, cp, s, (double*)dout.p,
+                                                      (int32_t*)dfl.p);
+  if ((e = cudaGetLastError()) != cudaSuccess) return err("k_contact_eval launch", e);
+  if ((e = cudaMemcpy(out, dout.p, sizeof(double) * 301 * n, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return err("k_contact_eval", e);
+  cudaMemcpy(flags, dfl.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+  return EB_OK;
+}

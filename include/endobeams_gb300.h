@@ -1,0 +1,168 @@
+/* endobeams_gb300 — C ABI of the GB300 (sm_103a) implementation of the
+ * EndoBeams.jl per-Newton-iteration hot path.
+ *
+ * Conventions
+ *   - Status: every entry point returns an int, 0 = EB_OK, negative = error;
+ *     eb_last_error() gives the message of the last failure on this thread.
+ *   - Ownership: host arrays are borrowed for the duration of the call and
+ *     copied; device memory belongs to the handle and is freed by eb_destroy.
+ *   - Indices are 0-based int64.  Node vectors are n x 3 row-major (node
+ *     major); rotation matrices are n x 9, each 3x3 column-major.
+ *   - Threads: one CUDA stream per handle; a handle is not thread-safe;
+ *     different handles may be used from different threads.
+ *   - Units follow the caller (the reference uses SI).
+ *
+ * Reference interfaces replaced (paths inside the EndoBeams.jl tree):
+ *   eb_create      — NodesBeams/Beams/BeamsConfiguration/RigidInteraction
+ *                    construction + setup_state_simulation + sparse_matrices_beams!
+ *                    + initialize_state_simulation!  (src/beams/def_node_beam.jl:55,
+ *                    src/beams/def_beam.jl:102, src/def_configurations.jl:15,
+ *                    src/inizialization.jl:17-45, src/sparse_matrices.jl:80)
+ *   eb_set_loads   — update_loads!            (src/utils_bcs_and_loads.jl:56-65)
+ *   eb_set_imposed — update_boundary_conditions! (src/utils_bcs_and_loads.jl:42-49)
+ *   eb_step        — solve_step_dynamics! = predictor! + corrector!
+ *                    (src/solve_step_dynamics.jl:1-14, src/predictor.jl:1-27,
+ *                    src/corrector.jl:1-59, with assemble! src/beams/assemble_beams.jl:1,
+ *                    assemble_contact! src/interactions/compute&assemble_interactions_beams.jl:447
+ *                    and the PARDISO solve src/linearsolvers.jl:2-28)
+ *   eb_commit      — update_converged!        (src/utils_solver.jl:252-275)
+ *   eb_rollback    — update_not_converged!    (src/utils_solver.jl:282-305)
+ *   eb_get_state / eb_set_state — the NodeBeam fields u, u̇, ü, w, ẇ, ẅ, R, ΔR
+ *                    (src/beams/def_node_beam.jl:6-48)
+ *   eb_element_eval — compute_beams           (src/beams/compute_beams.jl:1-538)
+ *   eb_contact_eval — compute_contact_beams   (src/interactions/compute&assemble_interactions_beams.jl:1-445)
+ */
+#ifndef ENDOBEAMS_GB300_H
+#define ENDOBEAMS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EB_OK 0
+#define EB_ERR_ARG (-1)
+#define EB_ERR_CUDA (-2)
+#define EB_ERR_NOMEM (-3)
+#define EB_ERR_STATE (-4)
+
+/* per-simulation status written by eb_step */
+#define EB_SIM_OK 0
+#define EB_SIM_NOT_CONVERGED 1     /* Newton reached max_iterations */
+#define EB_SIM_NAN 2               /* non-finite residual or increment */
+#define EB_SIM_KRYLOV_STAGNATED 3  /* linear solve missed its tolerance */
+
+/* linear solver precision */
+#define EB_PREC_FP64 0          /* FP64 GMRES */
+#define EB_PREC_MIXED 1         /* FP32 GMRES inside FP64 iterative refinement */
+
+/* SimulationParams (src/def_params.jl:1-35), hot-path fields, plus solver knobs. */
+typedef struct {
+  double alpha, beta, gamma;              /* HHT parameters */
+  double tolerance_residual;              /* Newton residual tolerance */
+  double tolerance_displacement;          /* Newton ‖ΔD‖ tolerance */
+  int32_t max_iterations;                 /* Newton iterations per step */
+  double gauss_w[3], gauss_z[3];          /* 3-point Gauss rule (def_params.jl:31-33) */
+  /* linear solver (replaces MKL PARDISO) */
+  int32_t precision;                      /* EB_PREC_FP64 | EB_PREC_MIXED */
+  int32_t krylov_restart;                 /* GMRES restart length m (<= 128) */
+  int32_t krylov_max_iter;                /* total GMRES iterations per solve */
+  double linear_tol;                      /* relative residual of each linear solve */
+  double inner_tol;                       /* relative tolerance of the FP32 inner solve (mixed) */
+  int32_t max_refinements;                /* FP64 refinement sweeps (mixed) */
+  int32_t threads_per_sim;                /* CTA size of the per-simulation solver, 0 = auto */
+} eb_params;
+
+/* Surface kinds */
+#define EB_SURFACE_NONE 0
+#define EB_SURFACE_SPHERE 1  /* SphereSurface (src/interactions/def_interactions.jl:30-33) */
+#define EB_SURFACE_SDF 2     /* DiscreteSignedDistanceField (def_interactions.jl:36-43,67-82) */
+
+/* One simulation: the arrays of NodesBeams, Beams, BoundaryConditions, Loads and RigidInteraction. */
+typedef struct {
+  int64_t n_nodes, n_elem;
+  const double *X0, *u, *ud, *udd, *w, *wd, *wdd; /* n x 3; NULL = zeros (X0 required) */
+  const double *R;                                /* n x 9 column-major; NULL = identity */
+  const int64_t *conn;                            /* n_elem x 2, 0-based node ids */
+  const double *E, *nu, *rho, *radius, *damping;  /* n_elem each */
+  const double *Re0;                              /* n_elem x 9 column-major; NULL = get_Rₑ⁰ */
+  int64_t n_fixed;                                /* BoundaryConditions.fixed_dofs */
+  const int64_t *fixed_dofs;                      /* 0-based, sorted ascending */
+  int64_t n_loaded;                               /* ConcentratedForce.loaded_dofs */
+  const int64_t *loaded_dofs;                     /* 0-based */
+  const double *fext0;                            /* n_loaded values of force_function(0, dof) */
+  /* contact (RigidInteraction) */
+  int32_t surface;                                /* EB_SURFACE_* */
+  double kn, mu, eps_t, eta_n;                    /* InteractionProperties (used fields) */
+  int64_t n_contact_elems;                        /* BeamElementSurface; 0 with NULL list = all */
+  const int64_t *contact_elems;
+  double sphere_center[3], sphere_radius;
+  int64_t sdf_dims[3];                            /* grid points nx, ny, nz */
+  double sdf_origin[3], sdf_spacing[3];
+  const double *sdf_values;                       /* nx*ny*nz, x fastest (VTK order) */
+  int32_t sdf_inside;                             /* 1: use values as given, 0: negate (def_interactions.jl:71) */
+} eb_sim_desc;
+
+typedef struct eb_handle eb_handle;
+
+/* Solver statistics of the last eb_step, per simulation. */
+typedef struct {
+  int32_t newton_iterations;   /* k - 1 */
+  int32_t krylov_iterations;   /* summed over the step's linear solves */
+  int32_t refinements;         /* FP64 refinement sweeps (mixed precision) */
+  int32_t status;              /* EB_SIM_* */
+  double last_res_norm, last_dD_norm;
+  double max_linear_rel_residual;  /* worst FP64 relative residual of the step's linear solves */
+} eb_sim_stats;
+
+const char *eb_last_error(void);
+
+int eb_default_params(eb_params *p);
+
+int eb_create(const eb_params *p, int32_t n_sims, const eb_sim_desc *sims, eb_handle **out);
+int eb_destroy(eb_handle *h);
+
+/* fext at t^{n+1} for the sim's loaded dofs (values of force_function(t, dof)). */
+int eb_set_loads(eb_handle *h, int32_t sim, const double *values);
+/* imposed displacements for the sim's fixed dofs (n_fixed values; Encastre entries 0). */
+int eb_set_imposed(eb_handle *h, int32_t sim, const double *values);
+
+/* One HHT step (predictor + Newton corrector) for every simulation with
+ * active[s] != 0 (active == NULL: all).  dt[s] per simulation.  k_out[s] is
+ * the reference's return value of corrector! (iterations + 1); a step with
+ * k_out[s] > max_iterations did not converge.  status_out may be NULL. */
+int eb_step(eb_handle *h, const double *dt, const int32_t *active, int32_t *k_out, int32_t *status_out);
+
+/* update_converged! / update_not_converged! for simulations with mask[s] != 0 (NULL: all). */
+int eb_commit(eb_handle *h, const int32_t *mask);
+int eb_rollback(eb_handle *h, const int32_t *mask);
+
+/* Node state of one simulation at n+1 (any pointer may be NULL). */
+int eb_get_state(eb_handle *h, int32_t sim, double *u, double *ud, double *udd, double *w, double *wd,
+                 double *wdd, double *R, double *dR);
+/* Node state at n (the last converged step). */
+int eb_get_state_n(eb_handle *h, int32_t sim, double *u, double *ud, double *udd, double *w, double *wd,
+                   double *wdd, double *R, double *dR);
+int eb_get_stats(eb_handle *h, eb_sim_stats *stats /* n_sims */);
+/* Assembled global vectors of one simulation at n+1 (6 n_nodes each; NULL to skip). */
+int eb_get_forces(eb_handle *h, int32_t sim, double *Tint, double *Tk, double *Tc);
+
+/* Testing entry points: evaluate single elements on the device.
+ * in:  n x 96 packed records (layout in the implementation notes), out: n x 458
+ * (strain, kinetic, Tint[12], Tk[12], K[144], M[144], C[144]; 12x12 column-major). */
+int eb_element_eval(int64_t n, const double *in, const double *gauss6, double *out);
+/* Contact: surf = [kind(0 sphere,1 sdf), cx, cy, cz, R, nx, ny, nz, x0, y0, z0, hx, hy, hz];
+ * values = SDF grid (x fastest) when kind = 1; props = [kn, mu, eps_t, eta_n];
+ * out n x 301 (energy, Tc[12], Kc[144], Cc[144]); flags[n] = 1 if any Gauss point touched. */
+int eb_contact_eval(int64_t n, const double *in, const double *gauss6, const double *props, const double *surf,
+                    const double *values, double *out, int32_t *flags);
+
+/* Device count and name probe (for hosts that must check before create). */
+int eb_device_info(int32_t *count, char *name, int32_t name_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ENDOBEAMS_GB300_H */

@@ -1,0 +1,68 @@
+"""Full HHT steps on the GPU (predictor + Newton corrector + GMRES) vs the oracle
+(same algorithm with an exact sparse LU).  Position parity bar: 1e-6 of the
+structure size."""
+import numpy as np
+import pytest
+
+import bridge
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_run(O, conf, params, inter, max_steps=None):
+    m = O.OracleModel(bridge.scene_from_conf(conf, inter), bridge.params_from(params))
+    r = O.run_simulation(m, max_steps=max_steps)
+    return m, r
+
+
+def test_cantilever_steps(eb, O, scenes):
+    conf, p, inter = scenes.cantilever(steps=40)
+    p.tolerance_residual = 1e-5
+    ref, rr = _oracle_run(O, conf, p, inter)
+    res = eb.run_simulation(conf, p, inter)
+    assert res.steps[0] == rr["steps"] == 40
+    assert res.ks[0] == rr["ks"]
+    err = np.abs(conf.nodes.un - ref.un).max()
+    assert err <= 1e-6 * 0.1, err
+    assert np.abs(conf.nodes.Rn - ref.Rn).max() <= 1e-6
+
+
+def test_frame_known_answer_gpu(eb, scenes):
+    """test/test_beams.jl:113-114 on the GPU: tip u_z at T = 0.15 ≈ -0.0100 (atol 1e-2)."""
+    conf, p, inter = scenes.frame_test_beams(T=0.15)
+    eb.run_simulation(conf, p, inter)
+    assert abs(conf.nodes.un[-1, 2] - (-0.0100)) <= 1e-2
+    assert abs(conf.nodes.un[-1, 2] - (-0.010034697661826674)) <= 1e-8  # oracle value
+
+
+def test_ring_drop_steps(eb, O, scenes):
+    conf, p, inter = scenes.ring_drop(steps=60)
+    p.tolerance_residual = 1e-5
+    ref, rr = _oracle_run(O, conf, p, inter)
+    res = eb.run_simulation(conf, p, inter)
+    assert res.steps[0] == rr["steps"]
+    err = np.abs(conf.nodes.un - ref.un).max()
+    assert err <= 1e-6 * 0.02, err
+
+
+def test_batch_matches_single(eb, scenes):
+    """A simulation's result does not depend on the other simulations in its batch (bitwise)."""
+    p = scenes.cantilever(steps=5)[1]
+    p.tolerance_residual = 1e-5
+    single = scenes.cantilever(steps=5)[0]
+    eb.run_simulation(single, p)
+    batch = [scenes.cantilever(steps=5)[0] for _ in range(3)] + [scenes.ring_drop(steps=5)[0]]
+    inters = [None, None, None, scenes.ring_drop(steps=5)[2]]
+    eb.run_simulations(batch, p, inters)
+    for c in batch[:3]:
+        assert np.array_equal(c.nodes.un, single.nodes.un)
+
+
+def test_rerun_bitwise(eb, scenes):
+    outs = []
+    for _ in range(2):
+        conf, p, inter = scenes.ring_drop(steps=10)
+        p.tolerance_residual = 1e-5
+        eb.run_simulation(conf, p, inter)
+        outs.append(conf.nodes.un.copy())
+    assert np.array_equal(outs[0], outs[1])
