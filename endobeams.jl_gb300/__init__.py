@@ -38,6 +38,13 @@ def contact_eval(inp: np.ndarray, props, surf, values=None, gauss: np.ndarray = 
     return out, flags
 
 
+def fp64_peak_tflops() -> float:
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    v = C.c_double(0.0)
+    check(_lib.load().eb_fp64_peak(C.byref(v)), "eb_fp64_peak")
+    return v.value
+
+
 __all__ = [
     "NodesBeams", "Beams", "BeamsConfiguration", "ConcentratedForce", "Loads", "Encastre", "ImposedDisplacement",
     "BoundaryConditions", "InteractionProperties", "SphereSurface", "PlaneSurface", "DiscreteSignedDistanceField",

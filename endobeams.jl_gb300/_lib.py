@@ -33,7 +33,7 @@ class EbParams(C.Structure):
         ("gauss_w", C.c_double * 3), ("gauss_z", C.c_double * 3),
         ("precision", C.c_int32), ("krylov_restart", C.c_int32), ("krylov_max_iter", C.c_int32),
         ("linear_tol", C.c_double), ("inner_tol", C.c_double),
-        ("max_refinements", C.c_int32), ("threads_per_sim", C.c_int32),
+        ("max_refinements", C.c_int32), ("threads_per_sim", C.c_int32), ("timing", C.c_int32),
     ]
 
 
@@ -80,7 +80,15 @@ SIGNATURES = {
     "eb_element_eval": (C.c_int, [C.c_int64, P_d, P_d, P_d]),
     "eb_contact_eval": (C.c_int, [C.c_int64, P_d, P_d, P_d, P_d, P_d, P_d, P_i32]),
     "eb_device_info": (C.c_int, [P_i32, C.c_char_p, C.c_int32]),
+    "eb_set_device": (C.c_int, [C.c_int32]),
+    "eb_timer_start": (C.c_int, [C.c_void_p]),
+    "eb_timer_stop": (C.c_int, [C.c_void_p, P_d]),
+    "eb_get_phase_times": (C.c_int, [C.c_void_p, P_d, P_i64, C.c_int32]),
+    "eb_set_loads_all": (C.c_int, [C.c_void_p, P_d]),
+    "eb_get_displacements": (C.c_int, [C.c_void_p, P_d]),
+    "eb_fp64_peak": (C.c_int, [P_d]),
 }
+PHASES = ("predictor", "beam", "contact", "assembly", "residual", "precond", "krylov", "update")
 
 _lib = None
 

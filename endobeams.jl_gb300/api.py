@@ -256,6 +256,7 @@ class SimulationParams:
     inner_tol: float = 1e-4
     max_refinements: int = 60
     threads_per_sim: int = 0
+    timing: bool = False             # per-phase CUDA-event timing inside each step
 
     def to_c(self) -> _lib.EbParams:
         p = _lib.default_params()
@@ -272,6 +273,7 @@ class SimulationParams:
         p.inner_tol = float(self.inner_tol)
         p.max_refinements = int(self.max_refinements)
         p.threads_per_sim = int(self.threads_per_sim)
+        p.timing = 1 if self.timing else 0
         return p
 
 
@@ -388,6 +390,40 @@ class GpuSimulations:
         out = {k: np.zeros(N) for k in ("Tint", "Tk", "Tc")}
         check(self.L.eb_get_forces(self.h, s, ptr(out["Tint"]), ptr(out["Tk"]), ptr(out["Tc"])), "eb_get_forces")
         return out
+
+    def loads_all(self, t_next) -> np.ndarray:
+        """Loaded-dof values of every simulation at its t^{n+1} (concatenated in simulation order)."""
+        vals = []
+        for s, conf in enumerate(self.confs):
+            cf = conf.loads.concentrated_force if conf.loads is not None else None
+            if cf is not None and len(cf.loaded_dofs):
+                t = float(np.broadcast_to(t_next, (self.n,))[s])
+                vals += [cf.force_function(t, int(i) + 1) for i in _dofs(cf.loaded_dofs)]
+        return f64(vals)
+
+    def set_loads_all(self, values: np.ndarray):
+        if len(values):
+            check(self.L.eb_set_loads_all(self.h, ptr(f64(values))), "eb_set_loads_all")
+
+    def displacements(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        total = sum(len(c.nodes) for c in self.confs)
+        out = np.zeros((total, 3)) if out is None else out
+        check(self.L.eb_get_displacements(self.h, ptr(out)), "eb_get_displacements")
+        return out
+
+    def timer_start(self):
+        check(self.L.eb_timer_start(self.h), "eb_timer_start")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double(0.0)
+        check(self.L.eb_timer_stop(self.h, C.byref(ms)), "eb_timer_stop")
+        return ms.value
+
+    def phase_times(self, reset: bool = False):
+        ms = np.zeros(8)
+        n = np.zeros(8, np.int64)
+        check(self.L.eb_get_phase_times(self.h, ptr(ms), ptr(n, C.c_int64), 1 if reset else 0), "eb_get_phase_times")
+        return dict(zip(_lib.PHASES, ms)), dict(zip(_lib.PHASES, n))
 
     def stats(self):
         check(self.L.eb_get_stats(self.h, self._stats), "eb_get_stats")

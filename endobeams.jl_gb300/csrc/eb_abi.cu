@@ -149,8 +149,53 @@ std::vector<double> eb_sdf_coefficients_host(const double* values, const int64_t
 }
 int eb_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 
+// ---------------------------------------------------------------- phase timing
+// CUDA events recorded on the handle's stream at phase boundaries; elapsed
+// times are resolved at the synchronisation points eb_step already has.
+struct PhaseTimer {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<int> phase_of;
+  int used = 0;
+  double ms[EB_NPHASES] = {0};
+  int64_t launches[EB_NPHASES] = {0};
+  void init(bool enable) {
+    on = enable;
+    if (!on) return;
+    pool.resize(96);
+    phase_of.assign(96, -1);
+    for (auto& e : pool) cudaEventCreate(&e);
+  }
+  void destroy() {
+    for (auto& e : pool) cudaEventDestroy(e);
+    pool.clear();
+  }
+  void begin(cudaStream_t s) {
+    if (!on) return;
+    cudaEventRecord(pool[0], s);
+    used = 1;
+  }
+  void mark(int phase, cudaStream_t s) {
+    if (!on || used >= (int)pool.size()) return;
+    cudaEventRecord(pool[used], s);
+    phase_of[used] = phase;
+    ++used;
+  }
+  void resolve() {  // call after the stream has been synchronised
+    if (!on || used < 1) return;
+    for (int i = 1; i < used; ++i) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, pool[i - 1], pool[i]) == cudaSuccess) ms[phase_of[i]] += t;
+    }
+    std::swap(pool[0], pool[used - 1]);
+    used = 1;
+  }
+};
+
 // ---------------------------------------------------------------- handle
 struct eb_handle {
+  PhaseTimer timer;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
   eb_params P;
   int n_sims = 0;
   cudaStream_t stream = nullptr;
@@ -200,9 +245,13 @@ int upload_mask(eb_handle* h, int* dst, const int32_t* mask) {
 int solve(eb_handle* h) {
   launch_block_jacobi(h->d, h->d_Dinv64, h->d_Dinv32, h->stream);
   CK(cudaGetLastError());
+  h->timer.mark(EB_PHASE_PRECOND, h->stream);
+  h->timer.launches[EB_PHASE_PRECOND] += 1;
   const bool fp32 = h->P.precision == EB_PREC_MIXED;
   int threads = h->P.threads_per_sim > 0 ? h->P.threads_per_sim : 256;
   CK(launch_gmres(h->sa, fp32, threads, h->stream));
+  h->timer.mark(EB_PHASE_KRYLOV, h->stream);
+  h->timer.launches[EB_PHASE_KRYLOV] += 1;
   return EB_OK;
 }
 
@@ -258,6 +307,9 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   h->n_sims = n_sims;
   for (int i = 0; i < 3; ++i) { h->gauss.w[i] = p->gauss_w[i]; h->gauss.z[i] = p->gauss_z[i]; }
   CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&h->t0));
+  CK(cudaEventCreate(&h->t1));
+  h->timer.init(p->timing != 0);
 
   // ---- sizes and offsets
   h->node_off.assign(n_sims + 1, 0);
@@ -592,7 +644,44 @@ int eb_destroy(eb_handle* h) {
     cudaStreamSynchronize(h->stream);
     cudaStreamDestroy(h->stream);
   }
+  h->timer.destroy();
+  if (h->t0) cudaEventDestroy(h->t0);
+  if (h->t1) cudaEventDestroy(h->t1);
   delete h;
+  return EB_OK;
+}
+
+int eb_set_device(int32_t device) {
+  CK(cudaSetDevice(device));
+  return EB_OK;
+}
+
+int eb_timer_start(eb_handle* h) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  CK(cudaEventRecord(h->t0, h->stream));
+  return EB_OK;
+}
+
+int eb_timer_stop(eb_handle* h, double* ms) {
+  if (!h || !ms) return fail(EB_ERR_ARG, "bad arguments");
+  CK(cudaEventRecord(h->t1, h->stream));
+  CK(cudaEventSynchronize(h->t1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->t0, h->t1));
+  *ms = t;
+  return EB_OK;
+}
+
+int eb_get_phase_times(eb_handle* h, double* ms, int64_t* launches, int32_t reset) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  for (int i = 0; i < EB_NPHASES; ++i) {
+    if (ms) ms[i] = h->timer.ms[i];
+    if (launches) launches[i] = h->timer.launches[i];
+    if (reset) {
+      h->timer.ms[i] = 0;
+      h->timer.launches[i] = 0;
+    }
+  }
   return EB_OK;
 }
 
@@ -604,6 +693,7 @@ static int set_values(eb_handle* h, int32_t sim, const double* values, const std
   if (!values) return fail(EB_ERR_ARG, "values is null");
   CK(cudaMemcpyAsync(h->d_vals, values, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   k_scatter<<<nblocks(n, 256), 256, 0, h->stream>>>(d_idx + o, h->d_vals, n, dst);
+  h->timer.launches[EB_PHASE_UPDATE] += 1;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->stream));
   return EB_OK;
@@ -617,6 +707,30 @@ int eb_set_loads(eb_handle* h, int32_t sim, const double* values) {
 int eb_set_imposed(eb_handle* h, int32_t sim, const double* values) {
   if (!h) return fail(EB_ERR_ARG, "null handle");
   return set_values(h, sim, values, h->fix_off, h->d_fix_dof, h->d.imposed);
+}
+
+int eb_set_loads_all(eb_handle* h, const double* values) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  const int64_t n = (int64_t)h->load_dof.size();
+  if (n == 0) return EB_OK;
+  if (!values) return fail(EB_ERR_ARG, "values is null");
+  CK(cudaMemcpyAsync(h->d_vals, values, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  k_scatter<<<nblocks(n, 256), 256, 0, h->stream>>>(h->d_load_dof, h->d_vals, n, h->d.fext1);
+  h->timer.launches[EB_PHASE_UPDATE] += 1;
+  CK(cudaGetLastError());
+  return EB_OK;
+}
+
+int eb_get_displacements(eb_handle* h, double* u) {
+  if (!h || !u) return fail(EB_ERR_ARG, "bad arguments");
+  const int64_t NN = h->d.n_nodes;
+  std::vector<double> tmp((size_t)NN);
+  for (int k = 0; k < 3; ++k) {
+    CK(cudaMemcpyAsync(tmp.data(), h->d.u + k * NN, sizeof(double) * NN, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int64_t i = 0; i < NN; ++i) u[3 * i + k] = tmp[i];
+  }
+  return EB_OK;
 }
 
 int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_out, int32_t* status_out) {
@@ -645,19 +759,28 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
   CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * S, st));
   CK(cudaMemsetAsync(h->d_relres, 0, sizeof(double) * S, st));
   const Dev& d = h->d;
+  PhaseTimer& T = h->timer;
+  T.begin(st);
 
   // ---- predictor! (predictor.jl:1-27)
   launch_init_predictor(d, st);
   launch_predictor_rhs(d, a, b, g, st);
   launch_apply_bc(d, st);
+  T.mark(EB_PHASE_PREDICTOR, st);
+  T.launches[EB_PHASE_PREDICTOR] += 4;
   int rc = solve(h);
   if (rc) return rc;
   launch_global_predictor(d, b, g, st);
   launch_local_predictor(d, b, g, st);
-
   // ---- corrector! (corrector.jl:1-59)
   launch_init_corrector(d, st);
+  T.mark(EB_PHASE_PREDICTOR, st);
+  T.launches[EB_PHASE_PREDICTOR] += 3;
   CK(cudaGetLastError());
+  if (T.on) {
+    CK(cudaStreamSynchronize(st));
+    T.resolve();
+  }
   std::vector<double> res(S, INFINITY), dn(S, INFINITY);
   std::vector<int> running(S);
   for (int s = 0; s < S; ++s) running[s] = act[s] && (1 <= P.max_iterations);
@@ -665,18 +788,33 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     bool any = false;
     for (int s = 0; s < S; ++s) any |= running[s] != 0;
     if (!any) break;
+    T.begin(st);
     CK(cudaMemcpyAsync(h->d_active, running.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    T.mark(EB_PHASE_UPDATE, st);
     launch_beam(d, h->gauss, st);
-    if (h->any_contact) launch_contact(d, h->gauss, st);
+    T.mark(EB_PHASE_BEAM, st);
+    T.launches[EB_PHASE_BEAM] += 1;
+    if (h->any_contact) {
+      launch_contact(d, h->gauss, st);
+      T.mark(EB_PHASE_CONTACT, st);
+      T.launches[EB_PHASE_CONTACT] += 1;
+    }
     launch_gather(d, a, h->any_contact, st);
+    T.mark(EB_PHASE_ASSEMBLY, st);
+    T.launches[EB_PHASE_ASSEMBLY] += 2;
     launch_corrector_rhs(d, a, st);
     launch_apply_bc(d, st);
+    T.mark(EB_PHASE_RESIDUAL, st);
+    T.launches[EB_PHASE_RESIDUAL] += 3;
     rc = solve(h);
     if (rc) return rc;
     launch_global_corrector(d, st);
     launch_local_corrector(d, b, g, st);
+    T.launches[EB_PHASE_UPDATE] += 2;
     CK(cudaMemcpyAsync(h->h_norms.data(), h->d_norms, sizeof(double) * 4 * S, cudaMemcpyDeviceToHost, st));
+    T.mark(EB_PHASE_UPDATE, st);
     CK(cudaStreamSynchronize(st));
+    T.resolve();
     for (int s = 0; s < S; ++s) {
       if (!running[s]) continue;
       const double* q = &h->h_norms[4 * s];
@@ -724,6 +862,7 @@ static int commit_impl(eb_handle* h, const int32_t* mask, bool commit) {
   int rc = upload_mask(h, h->d_mask, mask);
   if (rc) return rc;
   launch_commit(h->d, h->d_mask, commit, h->stream);
+  h->timer.launches[EB_PHASE_UPDATE] += 3;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->stream));
   return EB_OK;

@@ -134,3 +134,47 @@ extern "C" int eb_contact_eval(int64_t n, const double* in, const double* gauss6
   cudaMemcpy(flags, dfl.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
   return EB_OK;
 }
+
+// ---------------------------------------------------------------- FP64 throughput probe
+namespace {
+__global__ void k_fp64_fma(double* out, int iters, double b, double c) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6,
+         a7 = a0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+}
+}  // namespace
+
+extern "C" int eb_fp64_peak(double* tflops) {
+  if (!tflops) return EB_ERR_ARG;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 256, blocks = sms * 8, iters = 4096;
+  DBuf out;
+  cudaError_t e;
+  if ((e = cudaMalloc(&out.p, sizeof(double) * threads * blocks)) != cudaSuccess) return err("cudaMalloc", e);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_fp64_fma<<<blocks, threads>>>((double*)out.p, iters, 0.999999, 1e-7);  // warm-up
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(a);
+    k_fp64_fma<<<blocks, threads>>>((double*)out.p, iters, 0.999999, 1e-7);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if ((e = cudaGetLastError()) != cudaSuccess) return err("k_fp64_fma", e);
+  const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return EB_OK;
+}

@@ -72,6 +72,7 @@ typedef struct {
   double inner_tol;                       /* relative tolerance of the FP32 inner solve (mixed) */
   int32_t max_refinements;                /* FP64 refinement sweeps (mixed) */
   int32_t threads_per_sim;                /* CTA size of the per-simulation solver, 0 = auto */
+  int32_t timing;                         /* 1: record per-phase CUDA-event times in eb_step */
 } eb_params;
 
 /* Surface kinds */
@@ -127,6 +128,12 @@ int eb_destroy(eb_handle *h);
 int eb_set_loads(eb_handle *h, int32_t sim, const double *values);
 /* imposed displacements for the sim's fixed dofs (n_fixed values; Encastre entries 0). */
 int eb_set_imposed(eb_handle *h, int32_t sim, const double *values);
+/* update_loads! for every simulation at once: the loaded-dof values of all
+ * simulations concatenated in simulation order (one host-to-device copy). */
+int eb_set_loads_all(eb_handle *h, const double *values);
+/* Displacements u at n+1 of all simulations, concatenated in simulation order
+ * (sum of n_nodes rows x 3), in one device-to-host transfer per component. */
+int eb_get_displacements(eb_handle *h, double *u);
 
 /* One HHT step (predictor + Newton corrector) for every simulation with
  * active[s] != 0 (active == NULL: all).  dt[s] per simulation.  k_out[s] is
@@ -158,8 +165,35 @@ int eb_element_eval(int64_t n, const double *in, const double *gauss6, double *o
 int eb_contact_eval(int64_t n, const double *in, const double *gauss6, const double *props, const double *surf,
                     const double *values, double *out, int32_t *flags);
 
+/* Measured FP64 FMA throughput of device 0 in TFLOP/s (independent FMA
+ * chains on every SM, CUDA-event timed); the roofline denominator of the
+ * FP64-bound element kernels.  No reference counterpart. */
+int eb_fp64_peak(double *tflops);
+
 /* Device count and name probe (for hosts that must check before create). */
 int eb_device_info(int32_t *count, char *name, int32_t name_len);
+/* Selects the CUDA device for handles created afterwards on this thread (no
+ * reference counterpart: the reference has no device; one process per GPU). */
+int eb_set_device(int32_t device);
+
+/* Device timing on the handle's stream (CUDA events; no reference counterpart,
+ * the reference's equivalent is TimerOutputs, src/corrector.jl:7-42).
+ * eb_timer_start/stop bracket any sequence of calls; stop returns elapsed ms. */
+int eb_timer_start(eb_handle *h);
+int eb_timer_stop(eb_handle *h, double *ms);
+/* Per-phase device time (ms) and kernel-launch counts accumulated by eb_step
+ * since the last reset (phases: EB_PHASE_*); needs eb_params.timing = 1 for
+ * times, launch counts are always kept. */
+#define EB_PHASE_PREDICTOR 0
+#define EB_PHASE_BEAM 1
+#define EB_PHASE_CONTACT 2
+#define EB_PHASE_ASSEMBLY 3
+#define EB_PHASE_RESIDUAL 4
+#define EB_PHASE_PRECOND 5
+#define EB_PHASE_KRYLOV 6
+#define EB_PHASE_UPDATE 7
+#define EB_NPHASES 8
+int eb_get_phase_times(eb_handle *h, double *ms, int64_t *launches, int32_t reset);
 
 #ifdef __cplusplus
 }
