@@ -257,6 +257,8 @@ class SimulationParams:
     max_refinements: int = 60
     threads_per_sim: int = 0
     timing: bool = False             # per-phase CUDA-event timing inside each step
+    preconditioner: str = "band"     # "band" (FP32 band LU, RCM order) | "block_jacobi"
+    refactor_its: int = 16           # reuse the band LU until a solve needs more GMRES iterations (0: always refactor)
 
     def to_c(self) -> _lib.EbParams:
         p = _lib.default_params()
@@ -274,6 +276,8 @@ class SimulationParams:
         p.max_refinements = int(self.max_refinements)
         p.threads_per_sim = int(self.threads_per_sim)
         p.timing = 1 if self.timing else 0
+        p.preconditioner = 1 if self.preconditioner == "block_jacobi" else 0
+        p.refactor_its = int(self.refactor_its)
         return p
 
 

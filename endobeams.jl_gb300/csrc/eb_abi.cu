@@ -128,6 +128,80 @@ void prefilter_axis(double* c, const int64_t dims[3], int axis, std::vector<doub
     }
 }
 
+// Reverse Cuthill-McKee order of one simulation's node graph (neighbours in
+// increasing degree, root a pseudo-peripheral node of each component).
+// adj holds local neighbour lists (self excluded).  Returns the half
+// bandwidth in nodes of the permuted graph; pos[i] is node i's position.
+int rcm_order(const std::vector<std::vector<int>>& adj, std::vector<int>& pos) {
+  const int n = (int)adj.size();
+  std::vector<int> order;
+  order.reserve(n);
+  std::vector<char> seen(n, 0);
+  std::vector<int> level(n, -1), queue;
+  auto bfs = [&](int root, std::vector<int>& visited) {
+    visited.clear();
+    visited.push_back(root);
+    level[root] = 0;
+    int last = 0;
+    for (size_t h = 0; h < visited.size(); ++h) {
+      int v = visited[h];
+      for (int w : adj[v])
+        if (level[w] < 0) {
+          level[w] = level[v] + 1;
+          last = std::max(last, level[w]);
+          visited.push_back(w);
+        }
+    }
+    return last;
+  };
+  std::vector<int> comp;
+  for (int start = 0; start < n; ++start) {
+    if (seen[start]) continue;
+    int root = start;
+    // pseudo-peripheral root (George-Liu iteration)
+    int ecc = bfs(root, comp);
+    for (int it = 0; it < 8; ++it) {
+      int best = -1;
+      for (int v : comp)
+        if (level[v] == ecc && (best < 0 || adj[v].size() < adj[best].size())) best = v;
+      for (int v : comp) level[v] = -1;
+      int e2 = bfs(best, comp);
+      if (e2 <= ecc) {
+        for (int v : comp) level[v] = -1;
+        break;
+      }
+      ecc = e2;
+      root = best;
+      for (int v : comp) level[v] = -1;
+    }
+    // Cuthill-McKee from root
+    queue.clear();
+    queue.push_back(root);
+    seen[root] = 1;
+    for (size_t h = 0; h < queue.size(); ++h) {
+      int v = queue[h];
+      order.push_back(v);
+      std::vector<int> nb;
+      for (int w : adj[v])
+        if (!seen[w]) nb.push_back(w);
+      std::sort(nb.begin(), nb.end(), [&](int x, int y) {
+        return adj[x].size() != adj[y].size() ? adj[x].size() < adj[y].size() : x < y;
+      });
+      for (int w : nb) {
+        seen[w] = 1;
+        queue.push_back(w);
+      }
+    }
+  }
+  std::reverse(order.begin(), order.end());
+  pos.assign(n, 0);
+  for (int k = 0; k < n; ++k) pos[order[k]] = k;
+  int bw = 0;
+  for (int v = 0; v < n; ++v)
+    for (int w : adj[v]) bw = std::max(bw, std::abs(pos[v] - pos[w]));
+  return bw;
+}
+
 std::vector<double> sdf_coefficients(const double* values, const int64_t dims[3], bool negate) {
   const int64_t px = dims[0] + 2, py = dims[1] + 2, pz = dims[2] + 2;
   std::vector<double> c((size_t)(px * py * pz), 0.0);
@@ -224,6 +298,19 @@ struct eb_handle {
   double* d_relres = nullptr;
   std::vector<eb_sim_stats> stats;
   std::vector<double> h_norms;
+  // band-LU preconditioner
+  bool any_band = false, any_jacobi = false;
+  int max_b = 0;
+  size_t band_floats = 0;
+  BandDev band{};
+  int* d_blk_row = nullptr;
+  std::vector<int> band_b;  // per sim half bandwidth (0: block-Jacobi)
+  // factorisation reuse
+  int* d_refactor = nullptr;
+  std::vector<int> need_refactor, refactor_mask;
+  std::vector<double> dt_at_factor, cur_dt;
+  std::vector<int> cur_active;
+  int64_t factorizations = 0;
 };
 
 namespace {
@@ -243,10 +330,35 @@ int upload_mask(eb_handle* h, int* dst, const int32_t* mask) {
 }
 
 int solve(eb_handle* h) {
-  launch_block_jacobi(h->d, h->d_Dinv64, h->d_Dinv32, h->stream);
+  if (h->any_jacobi) {
+    launch_block_jacobi(h->d, h->d_Dinv64, h->d_Dinv32, h->stream);
+    h->timer.launches[EB_PHASE_PRECOND] += 1;
+  }
+  if (h->any_band) {
+    // refactorise the simulations whose factors are missing, stale (Δt changed) or slow (GMRES iterations)
+    bool any = false;
+    for (int s = 0; s < h->n_sims; ++s) {
+      int r = 0;
+      if (h->cur_active[s] && h->band_b[s] > 0)
+        r = h->need_refactor[s] || h->dt_at_factor[s] != h->cur_dt[s] || h->P.refactor_its <= 0;
+      h->refactor_mask[s] = r;
+      if (r) {
+        h->need_refactor[s] = 0;
+        h->dt_at_factor[s] = h->cur_dt[s];
+        ++h->factorizations;
+        any = true;
+      }
+    }
+    if (any) {
+      CK(cudaMemcpyAsync(h->d_refactor, h->refactor_mask.data(), sizeof(int) * h->n_sims, cudaMemcpyHostToDevice,
+                         h->stream));
+      launch_band_fill(h->d, h->band, h->d_blk_row, h->stream);
+      CK(launch_band_lu(h->d, h->band, h->max_b, h->stream));
+      h->timer.launches[EB_PHASE_PRECOND] += 3;
+    }
+  }
   CK(cudaGetLastError());
   h->timer.mark(EB_PHASE_PRECOND, h->stream);
-  h->timer.launches[EB_PHASE_PRECOND] += 1;
   const bool fp32 = h->P.precision == EB_PREC_MIXED;
   int threads = h->P.threads_per_sim > 0 ? h->P.threads_per_sim : 256;
   CK(launch_gmres(h->sa, fp32, threads, h->stream));
@@ -279,6 +391,9 @@ int eb_default_params(eb_params* p) {
   p->inner_tol = 1e-4;
   p->max_refinements = 60;
   p->threads_per_sim = 0;
+  p->timing = 0;
+  p->preconditioner = EB_PRECOND_BAND;
+  p->refactor_its = 16;
   return EB_OK;
 }
 
@@ -493,6 +608,32 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   }
   h->blk_off.assign(n_sims + 1, 0);
   for (int s = 0; s < n_sims; ++s) h->blk_off[s + 1] = row_ptr[h->node_off[s + 1]];
+  std::vector<int> blk_row(NB);
+  for (int64_t i = 0; i < NN; ++i)
+    for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) blk_row[k] = (int)i;
+
+  // ---- band-LU preconditioner plan: reverse Cuthill-McKee order per simulation
+  std::vector<int> pos_all(NN), node_at(NN);
+  std::vector<int64_t> band_off(n_sims + 1, 0);
+  h->band_b.assign(n_sims, 0);
+  const int bmax = ((227 * 1024) / 4 / kPanel - kPanel) / 2;  // shared-memory limit of k_band_lu
+  for (int s = 0; s < n_sims; ++s) {
+    const int64_t no = h->node_off[s], n = h->node_off[s + 1] - no;
+    std::vector<std::vector<int>> la(n);
+    for (int64_t i = 0; i < n; ++i)
+      for (int g : adj[no + i])
+        if (g != (int)(no + i)) la[i].push_back((int)(g - no));
+    std::vector<int> pos;
+    const int w = rcm_order(la, pos);
+    int b = 6 * w + 5;
+    if (p->preconditioner == EB_PRECOND_BLOCK_JACOBI || b > bmax) b = 0;
+    h->band_b[s] = b;
+    for (int64_t i = 0; i < n; ++i) {
+      pos_all[no + i] = pos[i];
+      node_at[no + pos[i]] = (int)(no + i);
+    }
+    band_off[s + 1] = band_off[s] + (b ? 6 * n * (2 * (int64_t)b + 1) : 0);
+  }
 
   // ---- device arenas
   Arena& A = h->arena;
@@ -580,7 +721,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   const bool fp32 = p->precision == EB_PREC_MIXED;
   CK(A.alloc(&h->d_Dinv64, NN * 36));
   CK(A.alloc(&h->d_Dinv32, NN * 36));
-  CK(A.alloc(&h->d_norms, 4 * (size_t)n_sims));
+  CK(A.alloc(&h->d_norms, 5 * (size_t)n_sims));
   CK(A.alloc(&h->d_its, n_sims)); CK(A.alloc(&h->d_refs, n_sims)); CK(A.alloc(&h->d_status, n_sims));
   CK(A.alloc(&h->d_relres, n_sims));
   SolverArgs& sa = h->sa;
@@ -621,7 +762,50 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   sa.relres = h->d_relres;
   sa.status = h->d_status;
   h->stats.assign(n_sims, eb_sim_stats{});
-  h->h_norms.assign(4 * (size_t)n_sims, 0.0);
+  h->h_norms.assign(5 * (size_t)n_sims, 0.0);
+
+  // ---- band storage (falls back to block-Jacobi when it would not fit in half the free memory)
+  {
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    size_t need = sizeof(float) * (size_t)band_off[n_sims];
+    if (need > fr / 2) {
+      std::fill(h->band_b.begin(), h->band_b.end(), 0);
+      std::fill(band_off.begin(), band_off.end(), 0);
+      need = 0;
+    }
+    for (int s = 0; s < n_sims; ++s) {
+      h->max_b = std::max(h->max_b, h->band_b[s]);
+      if (h->band_b[s]) h->any_band = true;
+      else h->any_jacobi = true;
+    }
+    int64_t *p_boff;
+    int *p_bw, *p_pos, *p_nat;
+    CK(A.upload(&p_boff, band_off));
+    CK(A.upload(&p_bw, h->band_b));
+    CK(A.upload(&p_pos, pos_all));
+    CK(A.upload(&p_nat, node_at));
+    CK(A.upload(&h->d_blk_row, blk_row));
+    h->band_floats = (size_t)band_off[n_sims];
+    float *p_band, *p_work, *p_li, *p_ui;
+    CK(A.alloc(&p_band, h->band_floats));
+    CK(A.alloc(&p_work, ND));
+    const size_t inv = h->any_band ? (size_t)inv_base(NN, n_sims) : 1;
+    CK(A.alloc(&p_li, inv));
+    CK(A.alloc(&p_ui, inv));
+    CK(A.alloc(&h->d_refactor, n_sims));
+    h->band = BandDev{p_band, p_boff, p_bw, p_pos, p_nat, p_work, p_li, p_ui, h->d_refactor};
+    sa.band = h->band;
+    h->need_refactor.assign(n_sims, 1);
+    h->refactor_mask.assign(n_sims, 0);
+    h->dt_at_factor.assign(n_sims, 0.0);
+    h->cur_dt.assign(n_sims, 0.0);
+    h->cur_active.assign(n_sims, 0);
+    int max_n = 0;
+    for (int s = 0; s < n_sims; ++s) max_n = std::max<int>(max_n, (int)(6 * (h->node_off[s + 1] - h->node_off[s])));
+    sa.max_n = max_n;
+    sa.x_in_smem = h->any_band && gmres_smem(m) + sizeof(float) * (size_t)max_n <= 200 * 1024;
+  }
 
   // ---- initialize_state_simulation! (inizialization.jl:37-44): beams only, matricesⁿ ← matricesⁿ⁺¹
   int rc = upload_mask(h.get(), h->d_active, nullptr);
@@ -744,6 +928,8 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     act[s] = active ? (active[s] != 0) : 1;
     if (act[s] && !(dt[s] > 0)) return fail(EB_ERR_ARG, "eb_step: dt[%d] must be positive", s);
     dts[s] = dt[s];
+    h->cur_dt[s] = dt[s];
+    h->cur_active[s] = act[s];
     cK[s] = 1 + a;
     cC[s] = g / (b * dt[s]);
     cM[s] = 1 / (b * (dt[s] * dt[s]));
@@ -811,13 +997,14 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     launch_global_corrector(d, st);
     launch_local_corrector(d, b, g, st);
     T.launches[EB_PHASE_UPDATE] += 2;
-    CK(cudaMemcpyAsync(h->h_norms.data(), h->d_norms, sizeof(double) * 4 * S, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h->h_norms.data(), h->d_norms, sizeof(double) * 5 * S, cudaMemcpyDeviceToHost, st));
     T.mark(EB_PHASE_UPDATE, st);
     CK(cudaStreamSynchronize(st));
     T.resolve();
     for (int s = 0; s < S; ++s) {
       if (!running[s]) continue;
-      const double* q = &h->h_norms[4 * s];
+      const double* q = &h->h_norms[5 * s];
+      if (h->P.refactor_its > 0 && q[4] > h->P.refactor_its) h->need_refactor[s] = 1;
       // compute_norms_corrector (utils_solver.jl:126-151)
       double dnorm = std::sqrt(q[0]);
       double rn = std::sqrt(q[1]);

@@ -18,6 +18,7 @@
 #include <cfloat>
 #include <type_traits>
 
+#include "eb_band.cuh"
 #include "eb_gmres.cuh"
 
 namespace eb {
@@ -108,6 +109,8 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   const T* Dm = std::is_same<T, double>::value ? reinterpret_cast<const T*>(a.Dinv64)
                                               : reinterpret_cast<const T*>(a.Dinv32);
   using TACC = T;
+  const bool use_band = a.band.bw != nullptr && a.band.bw[s] > 0;
+  float* xs = a.x_in_smem ? reinterpret_cast<float*>(red + 8 * 32) : nullptr;  // permuted solve vector
 
   double v1[1] = {0.0};
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -137,7 +140,8 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
       for (int j = 0; j < jmax; ++j) {
         T* vj = V + (int64_t)j * n;
         T* w = V + (int64_t)(j + 1) * n;
-        cta_prec<T, T, T>(Dm, n0, n, vj, Z);
+        if (use_band) band_solve<T, T>(a.band, s, n0, n, vj, Z, xs);
+        else cta_prec<T, T, T>(Dm, n0, n, vj, Z);
         __syncthreads();
         cta_spmv<T, T, T, TACC>(Am, a.row_ptr, a.col, n0, n, Z, w, fx);
         __syncthreads();
@@ -220,13 +224,18 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
         Z[i] = (T)acc;
       }
       __syncthreads();
-      for (int r = threadIdx.x; r < n; r += blockDim.x) {
-        const int nl = r / 6, kk = r % 6;
-        const T* Db = Dm + (n0 + nl) * 36 + kk;
-        double acc = 0.0;
+      if (use_band) {
+        band_solve<T, T>(a.band, s, n0, n, Z, Z, xs);
+        for (int r = threadIdx.x; r < n; r += blockDim.x) X[r] += (double)Z[r];
+      } else {
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+          const int nl = r / 6, kk = r % 6;
+          const T* Db = Dm + (n0 + nl) * 36 + kk;
+          double acc = 0.0;
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc += (double)Db[6 * j] * (double)Z[6 * nl + j];
-        X[r] += acc;
+          for (int j = 0; j < 6; ++j) acc += (double)Db[6 * j] * (double)Z[6 * nl + j];
+          X[r] += acc;
+        }
       }
       __syncthreads();
       // true FP64 residual R = b - Ktan X
@@ -262,10 +271,11 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   }
   block_sum<4>(q, red);
   if (threadIdx.x == 0) {
-    a.norms[4 * s + 0] = q[0];
-    a.norms[4 * s + 1] = q[1];
-    a.norms[4 * s + 2] = q[2];
-    a.norms[4 * s + 3] = q[3];
+    a.norms[5 * s + 0] = q[0];
+    a.norms[5 * s + 1] = q[1];
+    a.norms[5 * s + 2] = q[2];
+    a.norms[5 * s + 3] = q[3];
+    a.norms[5 * s + 4] = (double)its;  // iterations of this solve
     a.its[s] += its;
     a.refs[s] += refs;
     const double rel = bnorm > 0.0 ? rnorm / bnorm : 0.0;
@@ -323,7 +333,7 @@ void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream
 size_t gmres_smem(int m) { return sizeof(double) * ((size_t)(m + 1) * m + 4 * (size_t)m + 1 + 8 * 32); }
 
 cudaError_t launch_gmres(const SolverArgs& a, bool fp32, int threads, cudaStream_t s) {
-  const size_t smem = gmres_smem(a.m);
+  const size_t smem = gmres_smem(a.m) + (a.x_in_smem ? sizeof(float) * (size_t)a.max_n : 0);
   if (fp32) {
     cudaFuncSetAttribute(k_gmres<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_gmres<float><<<a.n_sims, threads, smem, s>>>(a);

@@ -1,6 +1,6 @@
 // Per-simulation GMRES solver interface (implementation in eb_gmres.cu).
 #pragma once
-#include "eb_internal.cuh"
+#include "eb_band.cuh"
 
 namespace eb {
 
@@ -26,11 +26,14 @@ struct SolverArgs {
   void* Z;               // n_dof work (double or float)
   int m, max_iter, max_ref;
   double tol, inner_tol;
-  double* norms;         // 4 per sim: |ΔD_free|², |r_free|², |f_free|², |f_fixed|²
+  double* norms;         // 5 per sim: |ΔD_free|², |r_free|², |f_free|², |f_fixed|², iterations of the solve
   int* its;              // per sim, accumulated
   int* refs;             // per sim, accumulated
   double* relres;        // per sim, max over the step
   int* status;           // per sim, max over the step
+  BandDev band;          // band-LU preconditioner (bw[s] == 0: block-Jacobi for that sim)
+  int x_in_smem;         // 1: the permuted solve vector lives in shared memory
+  int max_n;             // largest simulation, in DOFs
 };
 
 void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream_t s);

@@ -73,7 +73,14 @@ typedef struct {
   int32_t max_refinements;                /* FP64 refinement sweeps (mixed) */
   int32_t threads_per_sim;                /* CTA size of the per-simulation solver, 0 = auto */
   int32_t timing;                         /* 1: record per-phase CUDA-event times in eb_step */
+  int32_t preconditioner;                 /* EB_PRECOND_* */
+  int32_t refactor_its;                   /* band LU is reused until a solve needs more GMRES
+                                             iterations than this or Δt changes (0: refactorise every solve) */
 } eb_params;
+
+/* GMRES preconditioner */
+#define EB_PRECOND_BAND 0          /* FP32 band LU in reverse Cuthill-McKee order (block-Jacobi where it does not fit) */
+#define EB_PRECOND_BLOCK_JACOBI 1  /* LU of each node's 6x6 diagonal block */
 
 /* Surface kinds */
 #define EB_SURFACE_NONE 0

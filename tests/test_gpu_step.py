@@ -66,3 +66,27 @@ def test_rerun_bitwise(eb, scenes):
         eb.run_simulation(conf, p, inter)
         outs.append(conf.nodes.un.copy())
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_preconditioners_agree(eb, scenes):
+    """FP32 band-LU and 6x6 block-Jacobi preconditioning converge to the same steps."""
+    out = {}
+    for pc in ("band", "block_jacobi"):
+        conf, p, inter = scenes.ring_drop(steps=30)
+        p.tolerance_residual = 1e-5
+        p.preconditioner = pc
+        res = eb.run_simulation(conf, p, inter)
+        out[pc] = (conf.nodes.un.copy(), res.krylov_iterations[0], res.newton_iterations[0])
+    assert np.abs(out["band"][0] - out["block_jacobi"][0]).max() <= 1e-9 * 0.02
+    assert out["band"][1] < out["block_jacobi"][1]
+
+
+def test_mixed_precision_solver(eb, O, scenes):
+    """FP32 Krylov + FP64 refinement reaches the same steps as the oracle's exact solve."""
+    conf, p, inter = scenes.cantilever(steps=20)
+    p.tolerance_residual = 1e-5
+    p.precision = "mixed"
+    ref, rr = _oracle_run(O, conf, p, inter)
+    res = eb.run_simulation(conf, p, inter)
+    assert res.steps[0] == rr["steps"]
+    assert np.abs(conf.nodes.un - ref.un).max() <= 1e-6 * 0.1
