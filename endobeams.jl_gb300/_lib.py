@@ -88,7 +88,10 @@ SIGNATURES = {
     "eb_set_loads_all": (C.c_int, [C.c_void_p, P_d]),
     "eb_get_displacements": (C.c_int, [C.c_void_p, P_d]),
     "eb_fp64_peak": (C.c_int, [P_d]),
+    "eb_contact_eval_noalloc": (C.c_int, [C.c_int64, C.c_void_p, P_d, P_d, P_d, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]),
 }
+EB_NOALLOC_SDF_MAX_COEFS = 287496
 PHASES = ("predictor", "beam", "contact", "assembly", "residual", "precond", "krylov", "update")
 
 _lib = None

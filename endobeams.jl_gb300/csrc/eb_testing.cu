@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/endobeams_gb300.h"
@@ -132,6 +133,129 @@ extern "C" int eb_contact_eval(int64_t n, const double* in, const double* gauss6
   if ((e = cudaMemcpy(out, dout.p, sizeof(double) * 301 * n, cudaMemcpyDeviceToHost)) != cudaSuccess)
     return err("k_contact_eval", e);
   cudaMemcpy(flags, dfl.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+  return EB_OK;
+}
+
+// ---------------------------------------------------------------- contact evaluation without allocation
+// Variant of eb_contact_eval for callers that cannot allocate device memory
+// during the call (inside stream capture, or under a caller-owned memory
+// pool): the caller's device buffers are used directly, and the prefiltered
+// SDF coefficients go to the fixed array below instead of a cudaMalloc.
+namespace {
+
+__device__ __align__(256) double g_noalloc_coef[EB_NOALLOC_SDF_MAX_COEFS];
+
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices] = {nullptr};  // device address of g_noalloc_coef, per device ordinal
+
+__global__ void k_sdf_interior(const double* __restrict__ vals, int nx, int ny, int nz, double* __restrict__ c) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nx * ny * nz) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / ((int64_t)nx * ny));
+  c[(i + 1) + (int64_t)(nx + 2) * ((j + 1) + (int64_t)(ny + 2) * (k + 1))] = vals[t];
+}
+
+// One thread per grid line along `axis`: in-place solve of the quadratic
+// B-spline interpolation system ⅛c[i-1] + ¾c[i] + ⅛c[i+1] = y[i] with the
+// reflected ends (first/last diagonal 7/8), then the two pads c[0] = c[1],
+// c[n+1] = c[n].  Lines run over the padded range of axes already filtered.
+__global__ void k_sdf_prefilter_axis(double* c, int nx, int ny, int nz, int axis) {
+  const int64_t px = nx + 2, py = ny + 2;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int n;
+  int64_t base, stride;
+  if (axis == 0) {  // lines (j, k), interior j and k
+    if (t >= (int64_t)ny * nz) return;
+    const int64_t j = 1 + t % ny, k = 1 + t / ny;
+    n = nx; stride = 1; base = px * (j + py * k);
+  } else if (axis == 1) {  // lines (i, k), all i, interior k
+    if (t >= px * nz) return;
+    const int64_t i = t % px, k = 1 + t / px;
+    n = ny; stride = px; base = i + px * py * k;
+  } else {  // lines (i, j), all i and j
+    if (t >= px * py) return;
+    const int64_t i = t % px, j = t / px;
+    n = nz; stride = px * py; base = i + px * j;
+  }
+  double* y = c + base + stride;  // first interior point of the line
+  if (n > 1) {
+    double cpa[32];
+    double cp = 0.125 / 0.875;
+    cpa[0] = cp;
+    y[0] = y[0] / 0.875;
+    for (int i = 1; i < n; ++i) {
+      const bool last = i == n - 1;
+      const double m = (last ? 0.875 : 0.75) - 0.125 * cp;
+      y[i * stride] = (y[i * stride] - 0.125 * y[(i - 1) * stride]) / m;
+      cp = last ? 0.0 : 0.125 / m;
+      if (i < 32) cpa[i] = cp;
+    }
+    // beyond the first 32 rows the factor has converged to its fixed point
+    for (int i = n - 2; i >= 0; --i) y[i * stride] -= cpa[i < 32 ? i : 31] * y[(i + 1) * stride];
+  }
+  y[-stride] = y[0];
+  y[n * stride] = y[(n - 1) * stride];
+}
+
+}  // namespace
+
+extern "C" int eb_contact_eval_noalloc(int64_t n, const double* d_in, const double* gauss6, const double* props,
+                                       const double* surf, const double* d_sdf_values, double* d_out,
+                                       int32_t* d_flags, void* stream) {
+  if (n < 0 || !gauss6 || !props || !surf) return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad arguments");
+  if (n == 0) return EB_OK;
+  if (!d_in || !d_out || !d_flags) return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: null device buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  Gauss3 g;
+  for (int i = 0; i < 3; ++i) { g.w[i] = gauss6[i]; g.z[i] = gauss6[3 + i]; }
+  ContactProps cp{props[0], props[1], props[2], props[3]};
+  SurfaceDev s;
+  std::memset(&s, 0, sizeof(s));
+  s.kind = (int)surf[0];
+  s.cx = surf[1]; s.cy = surf[2]; s.cz = surf[3]; s.R = surf[4];
+  if (s.kind == 1) {
+    const int64_t nx = (int64_t)surf[5], ny = (int64_t)surf[6], nz = (int64_t)surf[7];
+    if (!d_sdf_values) return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: SDF values missing");
+    if (nx < 1 || ny < 1 || nz < 1 || !(surf[11] > 0) || !(surf[12] > 0) || !(surf[13] > 0))
+      return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad SDF grid");
+    if ((nx + 2) * (ny + 2) * (nz + 2) > (int64_t)EB_NOALLOC_SDF_MAX_COEFS)
+      return eb_internal_fail(EB_ERR_ARG,
+                              "eb_contact_eval_noalloc: SDF grid too large for the fixed coefficient array "
+                              "((nx+2)(ny+2)(nz+2) > EB_NOALLOC_SDF_MAX_COEFS = 287496)");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return err("cudaGetDevice", e);
+    if (dev < 0 || dev >= kMaxDevices) return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: device ordinal");
+    double* coef = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(g_noalloc_mu);
+      if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_coef);
+        if (e != cudaSuccess) return err("cudaGetSymbolAddress", e);
+        g_noalloc_ptr[dev] = (double*)p;
+      }
+      coef = g_noalloc_ptr[dev];
+    }
+    const int NX = (int)nx, NY = (int)ny, NZ = (int)nz;
+    const int64_t pts = nx * ny * nz;
+    k_sdf_interior<<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(d_sdf_values, NX, NY, NZ, coef);
+    k_sdf_prefilter_axis<<<(unsigned)((ny * nz + 127) / 128), 128, 0, st>>>(coef, NX, NY, NZ, 0);
+    k_sdf_prefilter_axis<<<(unsigned)(((nx + 2) * nz + 127) / 128), 128, 0, st>>>(coef, NX, NY, NZ, 1);
+    k_sdf_prefilter_axis<<<(unsigned)(((nx + 2) * (ny + 2) + 127) / 128), 128, 0, st>>>(coef, NX, NY, NZ, 2);
+    s.coef = coef;
+    s.nx = NX; s.ny = NY; s.nz = NZ;
+    s.x0 = surf[8]; s.y0 = surf[9]; s.z0 = surf[10];
+    s.ihx = 1.0 / surf[11]; s.ihy = 1.0 / surf[12]; s.ihz = 1.0 / surf[13];
+    s.xl = (NX - 1) * surf[11]; s.yl = (NY - 1) * surf[12]; s.zl = (NZ - 1) * surf[13];
+  }
+  // untouched elements leave zero records, as in eb_contact_eval
+  cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(double) * 301 * n, st);
+  if (e != cudaSuccess) return err("cudaMemsetAsync", e);
+  k_contact_eval<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, d_in, g, cp, s, d_out, d_flags);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return err("k_contact_eval (no-alloc) launch", e);
   return EB_OK;
 }
 

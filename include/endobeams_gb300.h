@@ -172,6 +172,28 @@ int eb_element_eval(int64_t n, const double *in, const double *gauss6, double *o
 int eb_contact_eval(int64_t n, const double *in, const double *gauss6, const double *props, const double *surf,
                     const double *values, double *out, int32_t *flags);
 
+/* Contact evaluation that allocates no memory.  No counterpart in the
+ * reference: it exists for callers that must not allocate device memory
+ * during a call — code running inside CUDA stream capture (where cudaMalloc
+ * is not allowed), hosts whose device memory is owned by their own pool
+ * allocator (a Julia or PyTorch runtime), and real-time loops that forbid
+ * allocation after start-up.  Same arithmetic and outputs as
+ * eb_contact_eval, but every pointer named d_* is DEVICE memory supplied by
+ * the caller (n x 96 inputs, the SDF grid, n x 301 outputs, n flags);
+ * gauss6, props and surf are small host arrays as in eb_contact_eval.
+ * The prefiltered SDF coefficients live in one fixed device array of
+ * EB_NOALLOC_SDF_MAX_COEFS doubles (2.3 MB, held on every GPU that loads
+ * the library until the process exits): grids with (nx+2)(ny+2)(nz+2)
+ * above that (64^3 points) are rejected with EB_ERR_ARG.  The first call on
+ * a device looks up that array's device address; make that first call
+ * before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (different streams, or different host threads) race.
+ * stream may be NULL (legacy default stream); the call is asynchronous. */
+#define EB_NOALLOC_SDF_MAX_COEFS 287496
+int eb_contact_eval_noalloc(int64_t n, const double *d_in, const double *gauss6, const double *props,
+                            const double *surf, const double *d_sdf_values, double *d_out, int32_t *d_flags,
+                            void *stream);
+
 /* Measured FP64 FMA throughput of device 0 in TFLOP/s (independent FMA
  * chains on every SM, CUDA-event timed); the roofline denominator of the
  * FP64-bound element kernels.  No reference counterpart. */
