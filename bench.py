@@ -35,9 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # FP64 floating-point operations the device beam kernel executes per element
-# evaluation (DADD + DMUL + 2·DFMA counted by ncu on the element kernel;
-# profiles/beam_kernel_nets.md).
-F_ELEM_FP64 = None
+# evaluation: 202 DADD + 368 DMUL + 714 DFMA counted by ncu's SASS counters on
+# k_beam (profiles/beam_kernel_nets16.md).
+F_ELEM_FP64 = 1998.0
 
 
 def parse():

@@ -1,0 +1,121 @@
+"""Host-side logic that needs no GPU: API semantics, scene generators, and the
+batched time loop's Δt policy against the oracle's restatement of
+run_simulation.jl:170-244 on scripted Newton outcomes."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+
+def test_boundary_conditions_semantics(eb):
+    bc = eb.BoundaryConditions(eb.Encastre(range(2, 7)), eb.ImposedDisplacement(1, lambda t: 2 * t), 126)
+    assert list(bc.fixed_dofs) == [0, 1, 2, 3, 4, 5]          # sorted union, 0-based
+    assert list(bc.displaced_indices) == [0]
+    assert len(bc.free_dofs) == 120
+    bc2 = eb.BoundaryConditions(12)
+    assert len(bc2.fixed_dofs) == 0 and len(bc2.free_dofs) == 12
+
+
+def test_beams_use_one_based_connectivity(eb):
+    X = np.zeros((3, 3))
+    X[:, 0] = [0, 1, 2]
+    nodes = eb.NodesBeams(X)
+    beams = eb.Beams(nodes, [(1, 2), (2, 3)], 1.0, 0.3, 1.0, 0.1, 0.0)
+    assert beams.conn.tolist() == [[0, 1], [1, 2]]
+    assert np.allclose(nodes.R, np.eye(3).flatten("F"))
+
+
+def test_scene_sizes(scenes):
+    conf, _, _ = scenes.cantilever()
+    assert len(conf.nodes) == 21 and len(conf.beams) == 20
+    conf, _, inter = scenes.ring_drop()
+    assert len(conf.nodes) == 64 and len(conf.beams) == 64 and inter.master.dims == (64, 64, 64)
+    for side in (20, 40):
+        conf, _, _ = scenes.net_on_sphere(side, sdf=scenes.sphere_sdf(n=8, h=1e-3))
+        assert len(conf.beams) == 2 * side * (side - 1)
+    conf, _, inter = scenes.braided_stent()
+    assert len(conf.beams) == 9600 and len(conf.nodes) == 8664  # 9648 nodes before merging 984 crossings
+    assert inter.master.dims == (96, 96, 256)
+    sides = scenes.net_sides(256, seed=0)
+    assert sides.min() >= 20 and sides.max() <= 40
+
+
+def test_stent_crossings_coincide(scenes):
+    conf, _, _ = scenes.braided_stent(wires=16, elems_per_wire=40)
+    X = conf.nodes.X0
+    # every node is used, and merged crossing nodes have four incident elements
+    deg = np.bincount(conf.beams.conn.ravel(), minlength=len(X))
+    assert deg.min() >= 1 and set(np.unique(deg)) <= {1, 2, 3, 4}
+    assert (deg == 4).sum() > 0
+
+
+class _ScriptedEngine:
+    """Stands in for GpuSimulations: returns scripted k per step and records the calls."""
+
+    def __init__(self, scripts):
+        self.scripts = [list(s) for s in scripts]
+        self.n = len(scripts)
+        self.calls = []
+
+    def set_time(self, s, t):
+        self.calls.append(("t", s, round(t, 12)))
+
+    def step(self, dt, active):
+        k = np.array([self.scripts[s].pop(0) if active[s] else 0 for s in range(self.n)], np.int32)
+        self.calls.append(("dt", tuple(np.round(dt, 15)), tuple(active)))
+        return k, np.zeros(self.n, np.int32)
+
+    def stats(self):
+        return [dict(newton_iterations=1, krylov_iterations=1)] * self.n
+
+    def commit(self, mask):
+        self.calls.append(("commit", tuple(mask)))
+
+    def rollback(self, mask):
+        self.calls.append(("rollback", tuple(mask)))
+
+    def sync_nodes(self):
+        pass
+
+
+class _ScriptedModel:
+    """Stands in for the oracle's OracleModel in oracle.run_simulation."""
+
+    def __init__(self, script, params):
+        self.script = list(script)
+        self.log = []
+        self.p = params
+
+    def step(self, t1, dt):
+        self.log.append((round(t1, 12), dt))
+        return self.script.pop(0)
+
+    def update_converged(self):
+        self.log.append("commit")
+
+    def update_not_converged(self):
+        self.log.append("rollback")
+
+
+@pytest.mark.parametrize("script", [
+    [3] * 12,                                   # steady: Δt grows ×1.5 after 4 successes (capped)
+    [3, 3, 21, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3],   # a failure halves Δt and rolls back
+    [9, 9, 9, 9, 9, 3, 3, 3, 3, 3, 3, 3],       # k > 8 blocks growth
+])
+def test_time_loop_policy_matches_reference(eb, script):
+    p = eb.SimulationParams(alpha=-0.05, beta=0.28, gamma=0.55, initial_timestep=0.01, min_timestep=1e-4,
+                            max_timestep=0.02, simulation_end_time=0.1, max_iterations=20)
+    eng = _ScriptedEngine([script + [3] * 50, script + [3] * 50])
+    res = eb.run_simulations([None, None], p, engine=eng)
+    op = O.Params(alpha=-0.05, beta=0.28, gamma=0.55, initial_timestep=0.01, min_timestep=1e-4, max_timestep=0.02,
+                  simulation_end_time=0.1, max_iterations=20)
+    om = _ScriptedModel(script + [3] * 50, op)
+    ores = O.run_simulation(om)
+    # same number of committed steps, same k sequence and same final time for every simulation
+    for s in range(2):
+        assert res.steps[s] == ores["steps"]
+        assert res.ks[s] == ores["ks"]
+        assert abs(res.t[s] - ores["t"]) < 1e-12
+    # same Δt sequence
+    dts = [c[1][0] for c in eng.calls if c[0] == "dt"]
+    assert np.allclose(dts, [d for (_, d) in [x for x in om.log if isinstance(x, tuple)]])
