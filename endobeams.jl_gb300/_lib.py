@@ -34,7 +34,7 @@ class EbParams(C.Structure):
         ("precision", C.c_int32), ("krylov_restart", C.c_int32), ("krylov_max_iter", C.c_int32),
         ("linear_tol", C.c_double), ("inner_tol", C.c_double),
         ("max_refinements", C.c_int32), ("threads_per_sim", C.c_int32), ("timing", C.c_int32),
-        ("preconditioner", C.c_int32), ("refactor_its", C.c_int32),
+        ("preconditioner", C.c_int32), ("refactor_its", C.c_int32), ("stage_band", C.c_int32),
     ]
 
 

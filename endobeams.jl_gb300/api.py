@@ -259,6 +259,7 @@ class SimulationParams:
     timing: bool = False             # per-phase CUDA-event timing inside each step
     preconditioner: str = "band"     # "band" (FP32 band LU, RCM order) | "block_jacobi"
     refactor_its: int = 16           # reuse the band LU until a solve needs more GMRES iterations (0: always refactor)
+    stage_band: bool = True          # stream band blocks into shared memory with bulk async copies
 
     def to_c(self) -> _lib.EbParams:
         p = _lib.default_params()
@@ -278,6 +279,7 @@ class SimulationParams:
         p.timing = 1 if self.timing else 0
         p.preconditioner = 1 if self.preconditioner == "block_jacobi" else 0
         p.refactor_its = int(self.refactor_its)
+        p.stage_band = int(bool(self.stage_band))
         return p
 
 

@@ -394,6 +394,7 @@ int eb_default_params(eb_params* p) {
   p->timing = 0;
   p->preconditioner = EB_PRECOND_BAND;
   p->refactor_its = 16;
+  p->stage_band = 1;
   return EB_OK;
 }
 
@@ -632,7 +633,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
       pos_all[no + i] = pos[i];
       node_at[no + pos[i]] = (int)(no + i);
     }
-    band_off[s + 1] = band_off[s] + (b ? 6 * n * (2 * (int64_t)b + 1) : 0);
+    band_off[s + 1] = band_off[s] + (b ? band_floats(6 * n, b) : 0);
   }
 
   // ---- device arenas
@@ -805,6 +806,12 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     for (int s = 0; s < n_sims; ++s) max_n = std::max<int>(max_n, (int)(6 * (h->node_off[s + 1] - h->node_off[s])));
     sa.max_n = max_n;
     sa.x_in_smem = h->any_band && gmres_smem(m) + sizeof(float) * (size_t)max_n <= 200 * 1024;
+    // stage band blocks through shared memory when the two buffers fit beside the rest
+    sa.stage_floats = 0;
+    if (h->any_band && p->stage_band) {
+      sa.stage_floats = kPanel * (h->max_b + 1);
+      if (gmres_smem_total(sa) > kGmresSmemLimit) sa.stage_floats = 0;
+    }
   }
 
   // ---- initialize_state_simulation! (inizialization.jl:37-44): beams only, matricesⁿ ← matricesⁿ⁺¹
@@ -1031,6 +1038,12 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     int stt = status[s];
     if (!std::isfinite(res[s]) || !std::isfinite(dn[s])) stt = EB_SIM_NAN;
     if (k[s] > P.max_iterations && stt == EB_SIM_OK) stt = EB_SIM_NOT_CONVERGED;
+    if (stt == EB_SIM_WAIT_TIMEOUT) {
+      // the step's solves are not trusted: report "not converged" (the caller rolls back)
+      // and read band blocks from global memory from now on
+      k[s] = P.max_iterations + 1;
+      h->sa.stage_floats = 0;
+    }
     q.newton_iterations = iter[s];
     q.krylov_iterations = its[s];
     q.refinements = refs[s];

@@ -20,7 +20,8 @@ __global__ void k_band_fill(Dev d, BandDev B, const int* __restrict__ blk_row) {
   const int64_t gr = 6 * (int64_t)row + r, gc = 6 * (int64_t)colnode + c;
   double v = d.Kt[t];
   if (d.fixed[gr] || d.fixed[gc]) v = (gr == gc) ? 1.0 : 0.0;
-  band_at(B.A + B.off[s], b, 2 * b + 1, i, j) = (float)v;
+  const int n = (int)(6 * (d.sim_node_off[s + 1] - d.sim_node_off[s]));
+  band_view(B, s, n).at(i, j) = (float)v;
 }
 
 // Zeroes the bands of the simulations about to be refactorised (one CTA per simulation).
@@ -28,7 +29,7 @@ __global__ void k_band_zero(Dev d, BandDev B) {
   const int s = blockIdx.x;
   if (!d.active[s] || !B.refactor[s] || B.bw[s] == 0) return;
   float* A = B.A + B.off[s];
-  const int64_t len = 6 * (d.sim_node_off[s + 1] - d.sim_node_off[s]) * (2 * (int64_t)B.bw[s] + 1);
+  const int64_t len = band_floats(6 * (d.sim_node_off[s + 1] - d.sim_node_off[s]), B.bw[s]);
   for (int64_t i = threadIdx.x; i < len; i += blockDim.x) A[i] = 0.f;
 }
 
@@ -52,8 +53,7 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
   if (b == 0) return;
   const int64_t n0 = d.sim_node_off[s];
   const int n = (int)(6 * (d.sim_node_off[s + 1] - n0));
-  const int64_t ld = 2 * b + 1;
-  float* A = B.A + B.off[s];
+  const BandView V = band_view(B, s, n);
   float* Li = B.Linv + inv_base(n0, s);  // per panel: kPanel x kPanel, column-major
   float* Ui = B.Uinv + inv_base(n0, s);
   extern __shared__ float smf[];
@@ -70,12 +70,12 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
     if (lane < kb)
       for (int r = warp; r < hp; r += nw) {
         const int i = k0 + r, j = k0 + lane;
-        P[r + ldp * lane] = (i - j <= b && j - i <= b) ? band_at(A, b, ld, i, j) : 0.f;
+        P[r + ldp * lane] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
       }
     for (int r = warp; r < kb; r += nw)
       for (int c = lane; c < q; c += 32) {
         const int i = k0 + r, j = k0 + kb + c;
-        U[r * b + c] = (j - i <= b) ? band_at(A, b, ld, i, j) : 0.f;
+        U[r * b + c] = (j - i <= b) ? V.at(i, j) : 0.f;
       }
     __syncthreads();
     // ---- 1. panel LU (column c = lane)
@@ -159,18 +159,18 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
       for (int c = 0; c < 4; ++c)
 #pragma unroll
         for (int a = 0; a < 4; ++a)
-          if (i0 + a < q && j0 + c < q) band_at(A, b, ld, k0 + kb + i0 + a, k0 + kb + j0 + c) -= acc[a][c];
+          if (i0 + a < q && j0 + c < q) V.at(k0 + kb + i0 + a, k0 + kb + j0 + c) -= acc[a][c];
     }
     // ---- write back panel and U12
     if (lane < kb)
       for (int r = warp; r < hp; r += nw) {
         const int i = k0 + r, j = k0 + lane;
-        if (i - j <= b && j - i <= b) band_at(A, b, ld, i, j) = P[r + ldp * lane];
+        if (i - j <= b && j - i <= b) V.at(i, j) = P[r + ldp * lane];
       }
     for (int r = warp; r < kb; r += nw)
       for (int c = lane; c < q; c += 32) {
         const int i = k0 + r, j = k0 + kb + c;
-        if (j - i <= b) band_at(A, b, ld, i, j) = U[r * b + c];
+        if (j - i <= b) V.at(i, j) = U[r * b + c];
       }
     __syncthreads();
   }

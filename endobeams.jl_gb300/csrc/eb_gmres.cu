@@ -111,6 +111,34 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   using TACC = T;
   const bool use_band = a.band.bw != nullptr && a.band.bw[s] > 0;
   float* xs = a.x_in_smem ? reinterpret_cast<float*>(red + 8 * 32) : nullptr;  // permuted solve vector
+  // shared-memory staging of band blocks for the triangular solves (bulk async copies)
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ int stage_fail;
+  __shared__ int stage_pend[2];
+  Stage stage;
+  const Stage* stp = nullptr;
+  uint32_t ph[2] = {0u, 0u};
+  if (use_band && a.stage_floats > 0) {
+    char* base = reinterpret_cast<char*>(xs ? xs + a.max_n : reinterpret_cast<float*>(red + 8 * 32));
+    base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 127) & ~uintptr_t(127));
+    float* f = reinterpret_cast<float*>(base);
+    stage.buf[0] = f;
+    stage.buf[1] = f + a.stage_floats;
+    stage.inv[0] = f + 2 * (int64_t)a.stage_floats;
+    stage.inv[1] = stage.inv[0] + kPanel * kPanel;
+    stage.bar = bars;
+    stage.fail = &stage_fail;
+    stage.pend = stage_pend;
+    if (threadIdx.x == 0) {
+      mbar_init(&bars[0], 1);
+      mbar_init(&bars[1], 1);
+      stage_fail = 0;
+      stage_pend[0] = stage_pend[1] = -1;
+      fence_async_smem();
+    }
+    __syncthreads();
+    stp = &stage;
+  }
 
   double v1[1] = {0.0};
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -140,7 +168,7 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
       for (int j = 0; j < jmax; ++j) {
         T* vj = V + (int64_t)j * n;
         T* w = V + (int64_t)(j + 1) * n;
-        if (use_band) band_solve<T, T>(a.band, s, n0, n, vj, Z, xs);
+        if (use_band) band_solve<T, T>(a.band, s, n0, n, vj, Z, xs, stp, ph);
         else cta_prec<T, T, T>(Dm, n0, n, vj, Z);
         __syncthreads();
         cta_spmv<T, T, T, TACC>(Am, a.row_ptr, a.col, n0, n, Z, w, fx);
@@ -225,7 +253,7 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
       }
       __syncthreads();
       if (use_band) {
-        band_solve<T, T>(a.band, s, n0, n, Z, Z, xs);
+        band_solve<T, T>(a.band, s, n0, n, Z, Z, xs, stp, ph);
         for (int r = threadIdx.x; r < n; r += blockDim.x) X[r] += (double)Z[r];
       } else {
         for (int r = threadIdx.x; r < n; r += blockDim.x) {
@@ -253,6 +281,11 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
       if (!isfinite(rnorm)) { status = 2; break; }
     }
     if (status == 0 && rnorm > target) status = 3;  // EB_SIM_KRYLOV_STAGNATED
+  }
+  __syncthreads();
+  if (stp && stage_fail) {
+    status = 4;  // EB_SIM_WAIT_TIMEOUT: a bulk copy did not complete in time
+    stage_drain(stp);
   }
 
   // ΔD[free] = x; Newton norms of compute_norms_corrector (utils_solver.jl:126-151)
@@ -332,8 +365,13 @@ void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream
 
 size_t gmres_smem(int m) { return sizeof(double) * ((size_t)(m + 1) * m + 4 * (size_t)m + 1 + 8 * 32); }
 
+size_t gmres_smem_total(const SolverArgs& a) {
+  return gmres_smem(a.m) + (a.x_in_smem ? sizeof(float) * (size_t)a.max_n : 0) +
+         (a.stage_floats > 0 ? 128 + sizeof(float) * (2 * (size_t)a.stage_floats + 2 * kPanel * kPanel) : 0);
+}
+
 cudaError_t launch_gmres(const SolverArgs& a, bool fp32, int threads, cudaStream_t s) {
-  const size_t smem = gmres_smem(a.m) + (a.x_in_smem ? sizeof(float) * (size_t)a.max_n : 0);
+  const size_t smem = gmres_smem_total(a);
   if (fp32) {
     cudaFuncSetAttribute(k_gmres<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_gmres<float><<<a.n_sims, threads, smem, s>>>(a);

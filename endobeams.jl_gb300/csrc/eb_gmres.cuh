@@ -34,10 +34,13 @@ struct SolverArgs {
   BandDev band;          // band-LU preconditioner (bw[s] == 0: block-Jacobi for that sim)
   int x_in_smem;         // 1: the permuted solve vector lives in shared memory
   int max_n;             // largest simulation, in DOFs
+  int stage_floats;      // > 0: band blocks staged in shared memory, floats per buffer (32 (b_max + 1))
 };
 
 void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream_t s);
 cudaError_t launch_gmres(const SolverArgs& a, bool fp32, int threads, cudaStream_t s);
 size_t gmres_smem(int m);
+size_t gmres_smem_total(const SolverArgs& a);  // dynamic shared memory of one launch
+constexpr size_t kGmresSmemLimit = 220 * 1024;  // leaves room for the kernel's static shared memory
 
 }  // namespace eb

@@ -162,9 +162,9 @@ def net_sides(count: int = 256, seed: int = 0):
 # ------------------------------------------------------------------ configurations 3 and 4
 
 def braided_stent(wires: int = 48, R: float = 4e-3, pitch_deg: float = 45.0, elems_per_wire: int = 200,
-                  crossing_every: int = 5, r: float = 5e-5, E: float = 5e10, rho: float = 6500.0,
-                  crimp_radius: float = 1.5e-3, cyl_radius: float = 3.5e-3, h: float = 1e-4,
-                  grid=(96, 96, 256), dt: float = 1e-5, steps: int = 10000, tol: float = 1e-8,
+                  crossing_every: Optional[int] = 5, length: Optional[float] = None, r: float = 5e-5, E: float = 5e10, rho: float = 6500.0,
+                  crimp_radius: Optional[float] = None, cyl_radius: float = 3.5e-3, h: float = 1e-4,
+                  grid: Optional[tuple] = (96, 96, 256), dt: float = 1e-5, steps: int = 10000, tol: float = 1e-8,
                   precision: str = "mixed", mu: float = 0.1):
     """Braided stent: wires/2 right- and wires/2 left-handed helices on radius R.
 
@@ -172,15 +172,27 @@ def braided_stent(wires: int = 48, R: float = 4e-3, pitch_deg: float = 45.0, ele
     a wire lies on a crossing with a wire of the other hand; those nodes are
     merged (shared).  The stent length follows: L = elems·(πR/tanφ)/(n·q)
     (n = wires/2, q = crossing_every), 20.9 mm for the default 48 wires at 45°.
+    With ``length`` given, q is the integer that brings L closest to it.
+    ``grid=None`` sizes the SDF grid (spacing h) to the stent: ±(max(R, cyl) +
+    0.5 mm) across and ±(L/2 + 1 mm) along the axis.
 
-    Crimp stand-in (no crimping procedure exists in the mounted reference): X₀
-    is the nominal stent; u⁰ maps it to radius ``crimp_radius`` with the axial
-    stretch that keeps helix arc length; R = I (the rotation factor of that
-    pure-stretch map); released at t = 0 inside a cylinder SDF
-    φ = cyl_radius − ρ (positive in the lumen)."""
+    Start (the reference has no crimping procedure): the stent is released at
+    t = 0, at rest and stress free at its nominal radius R, inside a cylinder
+    SDF φ = cyl_radius − ρ (positive in the lumen) of smaller radius, so the
+    vessel wall compresses the oversized stent through the penalty contact.
+
+    ``crimp_radius`` (optional) instead maps u⁰ to that radius with the axial
+    stretch that keeps helix arc length and R = I (the rotation factor of
+    that pure-stretch map).  With merged crossings this start is far from
+    equilibrium: every element next to a crossing carries an end-rotation
+    mismatch equal to the pitch change (about 30° for 4 → 1.5 mm), and the
+    resulting nodal accelerations (~1e9 m/s²) make the release diverge
+    within a few steps at Δt = 1e-5."""
     n = wires // 2
-    q = crossing_every
     tanp = math.tan(math.radians(pitch_deg))
+    if length is not None:
+        crossing_every = max(1, int(round(elems_per_wire * math.pi * R / (tanp * n * length))))
+    q = crossing_every
     dz = math.pi * R / (tanp * n * q)  # crossings every πR/(n tanφ) in z
     L = elems_per_wire * dz
     zs = dz * np.arange(elems_per_wire + 1)
@@ -206,14 +218,18 @@ def braided_stent(wires: int = 48, R: float = 4e-3, pitch_deg: float = 45.0, ele
     X = np.asarray(X)
     X[:, 2] -= L / 2
     conn0 = np.concatenate([np.stack([w[:-1], w[1:]], 1) for w in list(plus_ids) + list(minus_ids)])
-    # crimp displacement
-    rad = np.hypot(X[:, 0], X[:, 1])
-    sc = crimp_radius / R
-    stretch = math.sqrt(1 + tanp ** 2 * (1 - sc ** 2))
-    Xc = np.stack([X[:, 0] * sc, X[:, 1] * sc, X[:, 2] * stretch], 1)
-    nodes = NodesBeams(X, u0=Xc - X)
+    if crimp_radius is None:
+        nodes = NodesBeams(X)
+    else:
+        sc = crimp_radius / R
+        stretch = math.sqrt(1 + tanp ** 2 * (1 - sc ** 2))
+        Xc = np.stack([X[:, 0] * sc, X[:, 1] * sc, X[:, 2] * stretch], 1)
+        nodes = NodesBeams(X, u0=Xc - X)
     beams = Beams(nodes, conn0 + 1, E, 0.33, rho, r, 0.0)
     conf = BeamsConfiguration(nodes, beams, None, None)
+    if grid is None:
+        a = max(R, cyl_radius) + 0.5e-3
+        grid = (2 * int(math.ceil(a / h)) + 1,) * 2 + (2 * int(math.ceil((L / 2 + 1e-3) / h)) + 1,)
     nx, ny, nz = grid
     o = (-h * (nx - 1) / 2, -h * (ny - 1) / 2, -h * (nz - 1) / 2)
     sdf = grid_sdf(lambda x, y, z: cyl_radius - np.sqrt(x * x + y * y), o, h, grid)
@@ -225,7 +241,7 @@ def braided_stent(wires: int = 48, R: float = 4e-3, pitch_deg: float = 45.0, ele
 
 
 def stent_variants(count: int = 1024, seed: int = 2):
-    """Configuration 4 draws: wires ∈ {16,24,32,48}, R ∈ U[3,5] mm, pitch ∈ U[35,55]°,
+    """Stent-population draws: wires ∈ {16,24,32,48}, R ∈ U[3,5] mm, pitch ∈ U[35,55]°,
     elements per wire ∈ U{100..400}, cylinder radius ∈ U[0.85,0.95]·R."""
     rng = np.random.default_rng(seed)
     out = []
@@ -234,3 +250,11 @@ def stent_variants(count: int = 1024, seed: int = 2):
                         pitch_deg=float(rng.uniform(35, 55)), elems_per_wire=int(rng.integers(100, 401)),
                         cyl_frac=float(rng.uniform(0.85, 0.95))))
     return out
+
+
+def stent_variant(v: dict, steps: int = 10000, tol: float = 1e-8, precision: str = "mixed", length: float = 0.02):
+    """One stent of the population (a draw of ``stent_variants``): L ≈ 20 mm, its own
+    cylinder SDF of radius cyl_frac·R on a grid at 0.1 mm sized to the stent."""
+    return braided_stent(wires=v["wires"], R=v["R"], pitch_deg=v["pitch_deg"], elems_per_wire=v["elems_per_wire"],
+                         crossing_every=None, length=length, cyl_radius=v["cyl_frac"] * v["R"], grid=None,
+                         steps=steps, tol=tol, precision=precision)

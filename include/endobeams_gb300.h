@@ -52,6 +52,7 @@ extern "C" {
 #define EB_SIM_NOT_CONVERGED 1     /* Newton reached max_iterations */
 #define EB_SIM_NAN 2               /* non-finite residual or increment */
 #define EB_SIM_KRYLOV_STAGNATED 3  /* linear solve missed its tolerance */
+#define EB_SIM_WAIT_TIMEOUT 4      /* an asynchronous shared-memory copy did not complete within its wait limit */
 
 /* linear solver precision */
 #define EB_PREC_FP64 0          /* FP64 GMRES */
@@ -76,6 +77,8 @@ typedef struct {
   int32_t preconditioner;                 /* EB_PRECOND_* */
   int32_t refactor_its;                   /* band LU is reused until a solve needs more GMRES
                                              iterations than this or Δt changes (0: refactorise every solve) */
+  int32_t stage_band;                     /* 1: the triangular solves stream band blocks into shared memory
+                                             with bulk asynchronous copies (same arithmetic, same results) */
 } eb_params;
 
 /* GMRES preconditioner */

@@ -90,3 +90,19 @@ def test_mixed_precision_solver(eb, O, scenes):
     res = eb.run_simulation(conf, p, inter)
     assert res.steps[0] == rr["steps"]
     assert np.abs(conf.nodes.un - ref.un).max() <= 1e-6 * 0.1
+
+
+def test_staged_band_solve_bitwise(eb, scenes):
+    """Band blocks streamed into shared memory by bulk async copies give the same
+    arithmetic as reading them from global memory: identical steps, bit for bit,
+    on a net whose band spans many 32-column blocks."""
+    out = {}
+    for staged in (True, False):
+        conf, p, inter = scenes.net_on_sphere(24, steps=8, sdf=scenes.sphere_sdf(n=48, h=0.8e-3))
+        p.tolerance_residual = 1e-5
+        p.stage_band = staged
+        res = eb.run_simulation(conf, p, inter)
+        assert res.steps[0] == 8
+        out[staged] = (conf.nodes.un.copy(), res.krylov_iterations[0])
+    assert np.array_equal(out[True][0], out[False][0])
+    assert out[True][1] == out[False][1]
