@@ -23,6 +23,7 @@ SIM_STATUS = {0: "OK", 1: "NOT_CONVERGED", 2: "NAN", 3: "KRYLOV_STAGNATED"}
 P_d = C.POINTER(C.c_double)
 P_i64 = C.POINTER(C.c_int64)
 P_i32 = C.POINTER(C.c_int32)
+P_f = C.POINTER(C.c_float)
 
 
 class EbParams(C.Structure):
@@ -35,6 +36,7 @@ class EbParams(C.Structure):
         ("linear_tol", C.c_double), ("inner_tol", C.c_double),
         ("max_refinements", C.c_int32), ("threads_per_sim", C.c_int32), ("timing", C.c_int32),
         ("preconditioner", C.c_int32), ("refactor_its", C.c_int32), ("stage_band", C.c_int32),
+        ("warm_start", C.c_int32),
     ]
 
 
@@ -59,7 +61,8 @@ class EbSimStats(C.Structure):
     _fields_ = [
         ("newton_iterations", C.c_int32), ("krylov_iterations", C.c_int32), ("refinements", C.c_int32),
         ("status", C.c_int32), ("last_res_norm", C.c_double), ("last_dD_norm", C.c_double),
-        ("max_linear_rel_residual", C.c_double),
+        ("max_linear_rel_residual", C.c_double), ("warm_start_used", C.c_int32), ("reserved", C.c_int32),
+        ("predictor_rhs_norm", C.c_double), ("start_res_norm", C.c_double),
     ]
 
 
@@ -77,10 +80,18 @@ SIGNATURES = {
     "eb_get_state": (C.c_int, [C.c_void_p, C.c_int32] + [P_d] * 8),
     "eb_get_state_n": (C.c_int, [C.c_void_p, C.c_int32] + [P_d] * 8),
     "eb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(EbSimStats)]),
+    "eb_get_memory": (C.c_int, [C.c_void_p, P_i64, P_i32]),
     "eb_get_forces": (C.c_int, [C.c_void_p, C.c_int32, P_d, P_d, P_d]),
     "eb_element_eval": (C.c_int, [C.c_int64, P_d, P_d, P_d]),
     "eb_contact_eval": (C.c_int, [C.c_int64, P_d, P_d, P_d, P_d, P_d, P_d, P_i32]),
     "eb_device_info": (C.c_int, [P_i32, C.c_char_p, C.c_int32]),
+    "eb_rcm_order": (C.c_int, [C.c_int64, P_i64, P_i32, P_i32, P_i32]),
+    "eb_mlp_forward": (C.c_int, [P_f, P_f, C.c_int64, P_f]),
+    "eb_mlp_loss_grad": (C.c_int, [P_f, P_f, P_f, C.c_int64, P_d, P_f]),
+    "eb_mlp_train": (C.c_int, [P_f, P_f, P_f, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P_d]),
+    "eb_ws_set_model": (C.c_int, [C.c_void_p, P_f, P_f, P_f, P_f]),
+    "eb_ws_capture": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),
+    "eb_ws_samples": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P_f, P_f, P_i64]),
     "eb_set_device": (C.c_int, [C.c_int32]),
     "eb_timer_start": (C.c_int, [C.c_void_p]),
     "eb_timer_stop": (C.c_int, [C.c_void_p, P_d]),

@@ -260,6 +260,7 @@ class SimulationParams:
     preconditioner: str = "band"     # "band" (FP32 band LU, RCM order) | "block_jacobi"
     refactor_its: int = 16           # reuse the band LU until a solve needs more GMRES iterations (0: always refactor)
     stage_band: bool = True          # stream band blocks into shared memory with bulk async copies
+    warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start)
 
     def to_c(self) -> _lib.EbParams:
         p = _lib.default_params()
@@ -280,6 +281,9 @@ class SimulationParams:
         p.preconditioner = 1 if self.preconditioner == "block_jacobi" else 0
         p.refactor_its = int(self.refactor_its)
         p.stage_band = int(bool(self.stage_band))
+        if self.warm_start not in ("off", "learned"):
+            raise ValueError("warm_start must be 'off' or 'learned'")
+        p.warm_start = 1 if self.warm_start == "learned" else 0
         return p
 
 
@@ -304,6 +308,7 @@ class GpuSimulations:
         self.cparams = params.to_c()
         h = C.c_void_p()
         check(self.L.eb_create(C.byref(self.cparams), len(self.confs), descs, C.byref(h)), "eb_create")
+        self._keep = []  # host arrays are borrowed only for the duration of eb_create
         self.h = h
         self.n = len(self.confs)
         self._stats = (_lib.EbSimStats * self.n)()
@@ -430,6 +435,40 @@ class GpuSimulations:
         n = np.zeros(8, np.int64)
         check(self.L.eb_get_phase_times(self.h, ptr(ms), ptr(n, C.c_int64), 1 if reset else 0), "eb_get_phase_times")
         return dict(zip(_lib.PHASES, ms)), dict(zip(_lib.PHASES, n))
+
+    # ---- learned warm start
+    def set_warm_start(self, model):
+        """Installs a warm_start.WarmStartModel (None removes it)."""
+        f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+        if model is None:
+            check(self.L.eb_ws_set_model(self.h, None, None, None, None), "eb_ws_set_model")
+            return
+        P, a, b, o = f32(model.params), f32(model.in_shift), f32(model.in_scale), f32(model.out_scale)
+        check(self.L.eb_ws_set_model(self.h, ptr(P, C.c_float), ptr(a, C.c_float), ptr(b, C.c_float),
+                                     ptr(o, C.c_float)), "eb_ws_set_model")
+
+    def capture(self, capacity: int, stride: int = 1):
+        """Starts (capacity > 0) or stops (0) capturing training samples at each commit."""
+        check(self.L.eb_ws_capture(self.h, int(capacity), int(stride)), "eb_ws_capture")
+
+    def samples(self):
+        """(raw features n x 39, raw targets n x 6) captured so far; rows of uncommitted simulations are dropped."""
+        w = C.c_int64(0)
+        check(self.L.eb_ws_samples(self.h, 0, 0, None, None, C.byref(w)), "eb_ws_samples")
+        n = int(w.value)
+        F = np.zeros((n, 39), np.float32)
+        T = np.zeros((n, 6), np.float32)
+        if n:
+            check(self.L.eb_ws_samples(self.h, 0, n, ptr(F, C.c_float), ptr(T, C.c_float), C.byref(w)),
+                  "eb_ws_samples")
+        ok = np.isfinite(T).all(1) & np.isfinite(F).all(1)
+        return F[ok], T[ok]
+
+    def memory(self):
+        """(device bytes held by this batch, simulations preconditioned by the band LU)."""
+        b, n = C.c_int64(0), C.c_int32(0)
+        check(self.L.eb_get_memory(self.h, C.byref(b), C.byref(n)), "eb_get_memory")
+        return int(b.value), int(n.value)
 
     def stats(self):
         check(self.L.eb_get_stats(self.h, self._stats), "eb_get_stats")

@@ -9,11 +9,13 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/endobeams_gb300.h"
 #include "eb_gmres.cuh"
 #include "eb_internal.cuh"
+#include "eb_warm.cuh"
 
 using namespace eb;
 
@@ -159,6 +161,7 @@ int rcm_order(const std::vector<std::vector<int>>& adj, std::vector<int>& pos) {
     if (seen[start]) continue;
     int root = start;
     // pseudo-peripheral root (George-Liu iteration)
+    // (levels hold the BFS from `root` at the top of every iteration)
     int ecc = bfs(root, comp);
     for (int it = 0; it < 8; ++it) {
       int best = -1;
@@ -166,14 +169,11 @@ int rcm_order(const std::vector<std::vector<int>>& adj, std::vector<int>& pos) {
         if (level[v] == ecc && (best < 0 || adj[v].size() < adj[best].size())) best = v;
       for (int v : comp) level[v] = -1;
       int e2 = bfs(best, comp);
-      if (e2 <= ecc) {
-        for (int v : comp) level[v] = -1;
-        break;
-      }
+      if (e2 <= ecc) break;
       ecc = e2;
       root = best;
-      for (int v : comp) level[v] = -1;
     }
+    for (int v : comp) level[v] = -1;
     // Cuthill-McKee from root
     queue.clear();
     queue.push_back(root);
@@ -267,8 +267,32 @@ struct PhaseTimer {
 };
 
 // ---------------------------------------------------------------- handle
+// Learned warm start state of a handle (device buffers owned here).
+struct WsHost {
+  WsDev dev{};
+  int* d_nb = nullptr;         // n_nodes x 2 neighbours
+  int* d_surf_on = nullptr;    // per sim
+  float *F = nullptr, *X = nullptr, *Y = nullptr;
+  float *norm = nullptr;       // in_shift[48], in_scale[48], out_scale[6]
+  float* P = nullptr;          // network parameters (FP32)
+  __nv_bfloat16* W = nullptr;  // BF16 copy
+  bool model = false;
+  bool features_valid = false; // F holds this step's start (eb_step ran since the last commit/rollback)
+  // capture ring
+  float *sF = nullptr, *sT = nullptr;
+  int64_t cap = 0, cursor = 0, written = 0, phase = 0;
+  int stride = 1;
+  double* d_rn = nullptr;      // 2 n_sims residual norms
+  std::vector<double> rn;
+  std::vector<int> used;
+  ~WsHost() {
+    cudaFree(F); cudaFree(X); cudaFree(Y); cudaFree(norm); cudaFree(P); cudaFree(W); cudaFree(sF); cudaFree(sT);
+  }
+};
+
 struct eb_handle {
   PhaseTimer timer;
+  WsHost ws;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   eb_params P;
   int n_sims = 0;
@@ -329,7 +353,9 @@ int upload_mask(eb_handle* h, int* dst, const int32_t* mask) {
   return EB_OK;
 }
 
-int solve(eb_handle* h) {
+// Linear solve of the simulations active on the device; `mask` (host, n_sims)
+// marks the same simulations for the refactorisation decision.
+int solve(eb_handle* h, const int* mask) {
   if (h->any_jacobi) {
     launch_block_jacobi(h->d, h->d_Dinv64, h->d_Dinv32, h->stream);
     h->timer.launches[EB_PHASE_PRECOND] += 1;
@@ -339,7 +365,7 @@ int solve(eb_handle* h) {
     bool any = false;
     for (int s = 0; s < h->n_sims; ++s) {
       int r = 0;
-      if (h->cur_active[s] && h->band_b[s] > 0)
+      if (mask[s] && h->band_b[s] > 0)
         r = h->need_refactor[s] || h->dt_at_factor[s] != h->cur_dt[s] || h->P.refactor_its <= 0;
       h->refactor_mask[s] = r;
       if (r) {
@@ -395,6 +421,24 @@ int eb_default_params(eb_params* p) {
   p->preconditioner = EB_PRECOND_BAND;
   p->refactor_its = 16;
   p->stage_band = 1;
+  p->warm_start = EB_WS_OFF;
+  return EB_OK;
+}
+
+int eb_rcm_order(int64_t n, const int64_t* xadj, const int32_t* adjncy, int32_t* pos, int32_t* half_bandwidth) {
+  if (n < 0 || (n > 0 && (!xadj || !adjncy || !pos))) return fail(EB_ERR_ARG, "eb_rcm_order: bad arguments");
+  if (n >= (int64_t)INT32_MAX) return fail(EB_ERR_ARG, "eb_rcm_order: graph too large");
+  std::vector<std::vector<int>> adj((size_t)n);
+  for (int64_t v = 0; v < n; ++v)
+    for (int64_t k = xadj[v]; k < xadj[v + 1]; ++k) {
+      const int32_t w = adjncy[k];
+      if (w < 0 || w >= n) return fail(EB_ERR_ARG, "eb_rcm_order: neighbour out of range");
+      if (w != v) adj[(size_t)v].push_back(w);
+    }
+  std::vector<int> p;
+  const int bw = rcm_order(adj, p);
+  for (int64_t v = 0; v < n; ++v) pos[v] = p[(size_t)v];
+  if (half_bandwidth) *half_bandwidth = bw;
   return EB_OK;
 }
 
@@ -469,7 +513,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   std::vector<int> has_fixed(n_sims, 0);
   std::vector<SurfaceDev> surf(n_sims);
   std::vector<ContactProps> props(n_sims);
-  std::vector<std::vector<double>> sdf_coefs(n_sims);
+  std::vector<int> sdf_sims;  // simulations with a voxel SDF (coefficients computed below)
   h->load_off.assign(n_sims + 1, 0);
   h->fix_off.assign(n_sims + 1, 0);
 
@@ -544,7 +588,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
         sf.xl = (double)(sf.nx - 1) * S.sdf_spacing[0];
         sf.yl = (double)(sf.ny - 1) * S.sdf_spacing[1];
         sf.zl = (double)(sf.nz - 1) * S.sdf_spacing[2];
-        sdf_coefs[s] = sdf_coefficients(S.sdf_values, S.sdf_dims, S.sdf_inside == 0);
+        sdf_sims.push_back(s);
       }
     }
     // BCs and loads
@@ -656,13 +700,48 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   CK(A.alloc(&h->d_cM, n_sims));
   CK(A.alloc(&h->d_dt, n_sims));
   d.active = h->d_active; d.cK = h->d_cK; d.cC = h->d_cC; d.cM = h->d_cM; d.dt = h->d_dt;
-  // SDF coefficient grids
-  for (int s = 0; s < n_sims; ++s)
-    if (!sdf_coefs[s].empty()) {
-      double* c;
-      CK(A.upload(&c, sdf_coefs[s]));
-      surf[s].coef = c;
+  // SDF coefficient grids: simulations that pass the same grid (same values pointer,
+  // dims, spacing, origin and inside flag) share one device copy; distinct grids are
+  // prefiltered on host threads in chunks and uploaded as each chunk completes.
+  {
+    std::vector<int> owner(n_sims, -1), todo;
+    for (int s : sdf_sims) {
+      const eb_sim_desc& S = sims[s];
+      for (int t : todo) {
+        const eb_sim_desc& T = sims[t];
+        if (T.sdf_values == S.sdf_values && T.sdf_inside == S.sdf_inside &&
+            std::memcmp(T.sdf_dims, S.sdf_dims, sizeof S.sdf_dims) == 0 &&
+            std::memcmp(T.sdf_origin, S.sdf_origin, sizeof S.sdf_origin) == 0 &&
+            std::memcmp(T.sdf_spacing, S.sdf_spacing, sizeof S.sdf_spacing) == 0) {
+          owner[s] = t;
+          break;
+        }
+      }
+      if (owner[s] < 0) {
+        owner[s] = s;
+        todo.push_back(s);
+      }
     }
+    const int nthr = std::max(1, std::min<int>(16, (int)std::thread::hardware_concurrency()));
+    std::vector<std::vector<double>> chunk(nthr);
+    for (size_t c0 = 0; c0 < todo.size(); c0 += nthr) {
+      const size_t c1 = std::min(todo.size(), c0 + nthr);
+      std::vector<std::thread> pool;
+      for (size_t i = c0; i < c1; ++i)
+        pool.emplace_back([&, i] {
+          const eb_sim_desc& S = sims[todo[i]];
+          chunk[i - c0] = sdf_coefficients(S.sdf_values, S.sdf_dims, S.sdf_inside == 0);
+        });
+      for (auto& th : pool) th.join();
+      for (size_t i = c0; i < c1; ++i) {
+        double* c;
+        CK(A.upload(&c, chunk[i - c0]));
+        surf[todo[i]].coef = c;
+        std::vector<double>().swap(chunk[i - c0]);
+      }
+    }
+    for (int s : sdf_sims) surf[s].coef = surf[owner[s]].coef;
+  }
   SurfaceDev* p_surf;
   ContactProps* p_props;
   int* p_hf;
@@ -769,8 +848,11 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   {
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
+    // the band, its diagonal-block inverses and the work vector must leave 2 GB free
+    const size_t inv_bytes = 2 * sizeof(float) * (size_t)inv_base(NN, n_sims);
     size_t need = sizeof(float) * (size_t)band_off[n_sims];
-    if (need > fr / 2) {
+    const size_t margin = (size_t)2 << 30;
+    if (need + inv_bytes + margin > fr) {
       std::fill(h->band_b.begin(), h->band_b.end(), 0);
       std::fill(band_off.begin(), band_off.end(), 0);
       need = 0;
@@ -812,6 +894,24 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
       sa.stage_floats = kPanel * (h->max_b + 1);
       if (gmres_smem_total(sa) > kGmresSmemLimit) sa.stage_floats = 0;
     }
+  }
+
+  // ---- learned warm start: neighbour table and surface flags (buffers for features on first use)
+  {
+    std::vector<int> nb(2 * NN);
+    for (int64_t i = 0; i < NN; ++i) {
+      int q = 0;
+      for (int c : adj[i])
+        if (c != (int)i && q < 2) nb[2 * i + q++] = c;
+      for (; q < 2; ++q) nb[2 * i + q] = (int)i;
+    }
+    CK(A.upload(&h->ws.d_nb, nb));
+    CK(A.upload(&h->ws.d_surf_on, h->has_contact));
+    CK(A.alloc(&h->ws.d_rn, 2 * (size_t)n_sims));
+    h->ws.dev.nb = h->ws.d_nb;
+    h->ws.dev.surf_on = h->ws.d_surf_on;
+    h->ws.rn.assign(2 * (size_t)n_sims, 0.0);
+    h->ws.used.assign(n_sims, 0);
   }
 
   // ---- initialize_state_simulation! (inizialization.jl:37-44): beams only, matricesⁿ ← matricesⁿ⁺¹
@@ -924,10 +1024,58 @@ int eb_get_displacements(eb_handle* h, double* u) {
   return EB_OK;
 }
 
+// First Newton iteration from the learned start: simulations whose residual at
+// the learned start exceeds the HHT predictor's right-hand side (or is not
+// finite) go back to their committed node state and take the plain predictor
+// (predictor.jl:1-27) instead; then their first corrector assembly is redone.
+static int learned_start_check(eb_handle* h, const std::vector<int>& running, double a, double b, double g) {
+  WsHost& ws = h->ws;
+  const Dev& d = h->d;
+  const int S = h->n_sims;
+  cudaStream_t st = h->stream;
+  launch_ws_rnorm(d, ws.d_rn + S, st);
+  CK(cudaMemcpyAsync(ws.rn.data(), ws.d_rn, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<int> fb(S, 0);
+  bool any = false;
+  for (int s = 0; s < S; ++s) {
+    if (!running[s]) continue;
+    const double r0 = ws.rn[s], r1 = ws.rn[S + s];
+    fb[s] = !(std::isfinite(r1) && r1 <= r0);
+    ws.used[s] = !fb[s];
+    any |= fb[s] != 0;
+  }
+  if (!any) return EB_OK;
+  PhaseTimer& T = h->timer;
+  CK(cudaMemcpyAsync(h->d_active, fb.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->d_mask, fb.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  launch_restore_nodes(d, h->d_mask, st);
+  launch_init_predictor(d, st);
+  launch_predictor_rhs(d, a, b, g, st);
+  launch_apply_bc(d, st);
+  T.launches[EB_PHASE_PREDICTOR] += 4;
+  int rc = solve(h, fb.data());
+  if (rc) return rc;
+  launch_global_predictor(d, b, g, st);
+  launch_local_predictor(d, b, g, st);
+  launch_init_corrector(d, st);
+  launch_beam(d, h->gauss, st);
+  if (h->any_contact) launch_contact(d, h->gauss, st);
+  launch_gather(d, a, h->any_contact, st);
+  launch_corrector_rhs(d, a, st);
+  launch_apply_bc(d, st);
+  T.launches[EB_PHASE_PREDICTOR] += 9;
+  CK(cudaMemcpyAsync(h->d_active, running.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  CK(cudaGetLastError());
+  return EB_OK;
+}
+
 int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_out, int32_t* status_out) {
   if (!h || !dt || !k_out) return fail(EB_ERR_ARG, "eb_step: bad arguments");
   const int S = h->n_sims;
   const eb_params& P = h->P;
+  const bool learned = P.warm_start == EB_WS_LEARNED;
+  if (learned && !h->ws.model) return fail(EB_ERR_STATE, "eb_step: warm_start is EB_WS_LEARNED but no model is set");
   const double a = P.alpha, b = P.beta, g = P.gamma;
   std::vector<double> cK(S), cC(S), cM(S), dts(S);
   std::vector<int> act(S), iter(S, 0), k(S, 1);
@@ -955,14 +1103,30 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
   PhaseTimer& T = h->timer;
   T.begin(st);
 
+  // ---- features of the learned start / of the captured samples (committed state)
+  WsHost& ws = h->ws;
+  if (learned || ws.cap > 0) {
+    launch_ws_features(d, ws.dev, st);
+    T.launches[EB_PHASE_PREDICTOR] += 1;
+    ws.features_valid = true;
+  }
   // ---- predictor! (predictor.jl:1-27)
   launch_init_predictor(d, st);
   launch_predictor_rhs(d, a, b, g, st);
   launch_apply_bc(d, st);
   T.mark(EB_PHASE_PREDICTOR, st);
   T.launches[EB_PHASE_PREDICTOR] += 4;
-  int rc = solve(h);
-  if (rc) return rc;
+  int rc = 0;
+  if (learned) {
+    // the predictor's right-hand side norm is the fallback threshold; the network replaces its solve
+    launch_ws_rnorm(d, ws.d_rn, st);
+    CK(mlp_forward(MlpDev{ws.P, ws.W}, ws.X, d.n_nodes, ws.Y, st));
+    launch_ws_apply(d, ws.dev, st);
+    T.launches[EB_PHASE_PREDICTOR] += 3;
+  } else {
+    rc = solve(h, act.data());
+    if (rc) return rc;
+  }
   launch_global_predictor(d, b, g, st);
   launch_local_predictor(d, b, g, st);
   // ---- corrector! (corrector.jl:1-59)
@@ -977,6 +1141,8 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
   std::vector<double> res(S, INFINITY), dn(S, INFINITY);
   std::vector<int> running(S);
   for (int s = 0; s < S; ++s) running[s] = act[s] && (1 <= P.max_iterations);
+  bool first = true;
+  std::fill(ws.used.begin(), ws.used.end(), 0);
   while (true) {
     bool any = false;
     for (int s = 0; s < S; ++s) any |= running[s] != 0;
@@ -999,7 +1165,12 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     launch_apply_bc(d, st);
     T.mark(EB_PHASE_RESIDUAL, st);
     T.launches[EB_PHASE_RESIDUAL] += 3;
-    rc = solve(h);
+    if (learned && first) {
+      rc = learned_start_check(h, running, a, b, g);
+      if (rc) return rc;
+    }
+    first = false;
+    rc = solve(h, running.data());
     if (rc) return rc;
     launch_global_corrector(d, st);
     launch_local_corrector(d, b, g, st);
@@ -1051,6 +1222,9 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     q.last_res_norm = res[s];
     q.last_dD_norm = dn[s];
     q.max_linear_rel_residual = rel[s];
+    q.warm_start_used = learned ? ws.used[s] : 0;
+    q.predictor_rhs_norm = learned ? std::sqrt(ws.rn[s]) : 0.0;
+    q.start_res_norm = learned ? std::sqrt(ws.rn[S + s]) : 0.0;
     k_out[s] = k[s];
     if (status_out) status_out[s] = stt;
   }
@@ -1061,6 +1235,15 @@ static int commit_impl(eb_handle* h, const int32_t* mask, bool commit) {
   if (!h) return fail(EB_ERR_ARG, "null handle");
   int rc = upload_mask(h, h->d_mask, mask);
   if (rc) return rc;
+  WsHost& ws = h->ws;
+  if (commit && ws.cap > 0 && ws.features_valid) {
+    const int64_t per = (h->d.n_nodes + ws.stride - 1) / ws.stride;
+    launch_ws_capture(h->d, ws.dev, h->d_mask, ws.phase, ws.stride, ws.cursor, ws.cap, ws.sF, ws.sT, h->stream);
+    ws.cursor = (ws.cursor + per) % ws.cap;
+    ws.written = std::min(ws.cap, ws.written + per);
+    ws.phase += 1;
+  }
+  ws.features_valid = false;
   launch_commit(h->d, h->d_mask, commit, h->stream);
   h->timer.launches[EB_PHASE_UPDATE] += 3;
   CK(cudaGetLastError());
@@ -1103,6 +1286,107 @@ int eb_get_state_n(eb_handle* h, int32_t sim, double* u, double* ud, double* udd
 int eb_get_stats(eb_handle* h, eb_sim_stats* stats) {
   if (!h || !stats) return fail(EB_ERR_ARG, "bad arguments");
   std::memcpy(stats, h->stats.data(), sizeof(eb_sim_stats) * h->n_sims);
+  return EB_OK;
+}
+
+// Feature, input and output buffers of the learned start (allocated on first use).
+static int ws_buffers(eb_handle* h) {
+  WsHost& ws = h->ws;
+  if (ws.F) return EB_OK;
+  const size_t NN = (size_t)h->d.n_nodes;
+  CK(cudaMalloc(&ws.F, sizeof(float) * NN * kWsRaw));
+  CK(cudaMalloc(&ws.X, sizeof(float) * NN * kMlpIn));
+  CK(cudaMalloc(&ws.Y, sizeof(float) * NN * kMlpOut));
+  CK(cudaMalloc(&ws.norm, sizeof(float) * (2 * kMlpIn + kMlpOut)));
+  CK(cudaMemset(ws.F, 0, sizeof(float) * NN * kWsRaw));
+  CK(cudaMemset(ws.X, 0, sizeof(float) * NN * kMlpIn));
+  CK(cudaMemset(ws.Y, 0, sizeof(float) * NN * kMlpOut));
+  // identity normalisation until a model is set
+  std::vector<float> nm(2 * kMlpIn + kMlpOut, 0.f);
+  for (int k = kMlpIn; k < 2 * kMlpIn + kMlpOut; ++k) nm[k] = 1.f;
+  CK(cudaMemcpy(ws.norm, nm.data(), sizeof(float) * nm.size(), cudaMemcpyHostToDevice));
+  ws.dev.F = ws.F;
+  ws.dev.X = ws.X;
+  ws.dev.Y = ws.Y;
+  ws.dev.in_shift = ws.norm;
+  ws.dev.in_scale = ws.norm + kMlpIn;
+  ws.dev.out_scale = ws.norm + 2 * kMlpIn;
+  h->arena.bytes += sizeof(float) * NN * (kWsRaw + kMlpIn + kMlpOut);
+  return EB_OK;
+}
+
+int eb_ws_set_model(eb_handle* h, const float* params, const float* in_shift, const float* in_scale,
+                    const float* out_scale) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  WsHost& ws = h->ws;
+  if (!params) {
+    ws.model = false;
+    return EB_OK;
+  }
+  if (!in_shift || !in_scale || !out_scale) return fail(EB_ERR_ARG, "eb_ws_set_model: normalisation arrays missing");
+  for (int k = 0; k < kMlpIn; ++k)
+    if (!(in_scale[k] != 0.f) || !std::isfinite(in_scale[k]) || !std::isfinite(in_shift[k]))
+      return fail(EB_ERR_ARG, "eb_ws_set_model: in_scale must be finite and non-zero");
+  for (int k = 0; k < kMlpParams; ++k)
+    if (!std::isfinite(params[k])) return fail(EB_ERR_ARG, "eb_ws_set_model: non-finite parameter %d", k);
+  int rc = ws_buffers(h);
+  if (rc) return rc;
+  if (!ws.P) {
+    CK(cudaMalloc(&ws.P, sizeof(float) * kMlpParams));
+    CK(cudaMalloc(&ws.W, sizeof(__nv_bfloat16) * kMlpParams));
+  }
+  std::vector<float> nm(2 * kMlpIn + kMlpOut);
+  std::memcpy(nm.data(), in_shift, sizeof(float) * kMlpIn);
+  std::memcpy(nm.data() + kMlpIn, in_scale, sizeof(float) * kMlpIn);
+  std::memcpy(nm.data() + 2 * kMlpIn, out_scale, sizeof(float) * kMlpOut);
+  CK(cudaMemcpyAsync(ws.norm, nm.data(), sizeof(float) * nm.size(), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(ws.P, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, h->stream));
+  CK(mlp_to_bf16(ws.P, ws.W, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  ws.model = true;
+  return EB_OK;
+}
+
+int eb_ws_capture(eb_handle* h, int64_t capacity, int32_t stride) {
+  if (!h || capacity < 0 || stride < 1) return fail(EB_ERR_ARG, "eb_ws_capture: bad arguments");
+  WsHost& ws = h->ws;
+  CK(cudaStreamSynchronize(h->stream));
+  cudaFree(ws.sF);
+  cudaFree(ws.sT);
+  ws.sF = ws.sT = nullptr;
+  ws.cap = ws.cursor = ws.written = ws.phase = 0;
+  if (capacity == 0) return EB_OK;
+  int rc = ws_buffers(h);
+  if (rc) return rc;
+  CK(cudaMalloc(&ws.sF, sizeof(float) * (size_t)capacity * kWsRaw));
+  CK(cudaMalloc(&ws.sT, sizeof(float) * (size_t)capacity * kMlpOut));
+  ws.cap = capacity;
+  ws.stride = stride;
+  return EB_OK;
+}
+
+int eb_ws_samples(eb_handle* h, int64_t first, int64_t n, float* features, float* targets, int64_t* written) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  WsHost& ws = h->ws;
+  if (written) *written = ws.written;
+  if (n == 0) return EB_OK;
+  if (first < 0 || n < 0 || first + n > ws.cap) return fail(EB_ERR_ARG, "eb_ws_samples: range outside the ring");
+  CK(cudaStreamSynchronize(h->stream));
+  if (features)
+    CK(cudaMemcpy(features, ws.sF + first * kWsRaw, sizeof(float) * n * kWsRaw, cudaMemcpyDeviceToHost));
+  if (targets)
+    CK(cudaMemcpy(targets, ws.sT + first * kMlpOut, sizeof(float) * n * kMlpOut, cudaMemcpyDeviceToHost));
+  return EB_OK;
+}
+
+int eb_get_memory(eb_handle* h, int64_t* device_bytes, int32_t* band_sims) {
+  if (!h) return fail(EB_ERR_ARG, "null handle");
+  if (device_bytes) *device_bytes = (int64_t)h->arena.bytes;
+  if (band_sims) {
+    int c = 0;
+    for (int b : h->band_b) c += b > 0;
+    *band_sims = c;
+  }
   return EB_OK;
 }
 

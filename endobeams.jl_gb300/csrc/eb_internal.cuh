@@ -102,5 +102,7 @@ void launch_init_corrector(const Dev& d, cudaStream_t s);
 void launch_global_corrector(const Dev& d, cudaStream_t s);
 void launch_local_corrector(const Dev& d, double beta, double gamma, cudaStream_t s);
 void launch_commit(const Dev& d, const int* mask, bool commit, cudaStream_t s);
+// node state at n+1 <- node state at n (the node part of update_not_converged!)
+void launch_restore_nodes(const Dev& d, const int* mask, cudaStream_t s);
 
 }  // namespace eb

@@ -435,4 +435,8 @@ void launch_commit(const Dev& d, const int* mask, bool commit, cudaStream_t s) {
   if (d.nnzb) k_commit_blocks<<<nblocks(d.nnzb * 36, 256), 256, 0, s>>>(d, mask, commit ? 1 : 0);
 }
 
+void launch_restore_nodes(const Dev& d, const int* mask, cudaStream_t s) {
+  if (d.n_nodes) k_commit_nodes<<<nblocks(d.n_nodes), kThreads, 0, s>>>(d, mask, 0);
+}
+
 }  // namespace eb

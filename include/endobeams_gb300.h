@@ -79,7 +79,13 @@ typedef struct {
                                              iterations than this or Δt changes (0: refactorise every solve) */
   int32_t stage_band;                     /* 1: the triangular solves stream band blocks into shared memory
                                              with bulk asynchronous copies (same arithmetic, same results) */
+  int32_t warm_start;                     /* EB_WS_OFF | EB_WS_LEARNED (needs eb_ws_set_model) */
 } eb_params;
+
+/* Newton start of each step */
+#define EB_WS_OFF 0      /* HHT predictor (predictor.jl:1-27) */
+#define EB_WS_LEARNED 1  /* per-node MLP increment; per simulation, the predictor again when the learned
+                            start's residual exceeds the predictor's right-hand side */
 
 /* GMRES preconditioner */
 #define EB_PRECOND_BAND 0          /* FP32 band LU in reverse Cuthill-McKee order (block-Jacobi where it does not fit) */
@@ -125,6 +131,10 @@ typedef struct {
   int32_t status;              /* EB_SIM_* */
   double last_res_norm, last_dD_norm;
   double max_linear_rel_residual;  /* worst FP64 relative residual of the step's linear solves */
+  int32_t warm_start_used;         /* 1: the step started from the learned increment */
+  int32_t reserved;
+  double predictor_rhs_norm;       /* ‖r_free‖ of the HHT predictor's right-hand side (learned mode) */
+  double start_res_norm;           /* ‖r_free‖ at the learned start (learned mode) */
 } eb_sim_stats;
 
 const char *eb_last_error(void);
@@ -162,6 +172,8 @@ int eb_get_state(eb_handle *h, int32_t sim, double *u, double *ud, double *udd, 
 int eb_get_state_n(eb_handle *h, int32_t sim, double *u, double *ud, double *udd, double *w, double *wd,
                    double *wdd, double *R, double *dR);
 int eb_get_stats(eb_handle *h, eb_sim_stats *stats /* n_sims */);
+/* Device memory the handle holds (bytes), and how many simulations use the band-LU preconditioner. */
+int eb_get_memory(eb_handle *h, int64_t *device_bytes, int32_t *band_sims);
 /* Assembled global vectors of one simulation at n+1 (6 n_nodes each; NULL to skip). */
 int eb_get_forces(eb_handle *h, int32_t sim, double *Tint, double *Tk, double *Tc);
 
@@ -202,6 +214,11 @@ int eb_contact_eval_noalloc(int64_t n, const double *d_in, const double *gauss6,
  * FP64-bound element kernels.  No reference counterpart. */
 int eb_fp64_peak(double *tflops);
 
+/* Host only: the reverse Cuthill-McKee node order the band-LU preconditioner
+ * uses (CSR adjacency, self loops ignored); pos[v] = position of node v,
+ * *half_bandwidth = max |pos[v] - pos[w]| over edges.  No reference counterpart
+ * (the reference hands the matrix to PARDISO, src/linearsolvers.jl:15-23). */
+int eb_rcm_order(int64_t n, const int64_t *xadj, const int32_t *adjncy, int32_t *pos, int32_t *half_bandwidth);
 /* Device count and name probe (for hosts that must check before create). */
 int eb_device_info(int32_t *count, char *name, int32_t name_len);
 /* Selects the CUDA device for handles created afterwards on this thread (no
@@ -226,6 +243,42 @@ int eb_timer_stop(eb_handle *h, double *ms);
 #define EB_PHASE_UPDATE 7
 #define EB_NPHASES 8
 int eb_get_phase_times(eb_handle *h, double *ms, int64_t *launches, int32_t reset);
+
+/* ---------------------------------------------------------------- learned Newton warm start
+ * No reference counterpart: the reference starts every Newton loop from the
+ * HHT predictor (src/predictor.jl:1-27), which stays the fallback here.
+ *
+ * Per-node MLP: EB_WS_NIN normalised features -> 128 -> 128 -> EB_WS_NOUT,
+ * SiLU activations, BF16 weights, FP32 activations and accumulation.
+ * Parameter vector (EB_WS_NPARAMS floats): W1 [48 x 128] row-major, b1[128],
+ * W2 [128 x 128], b2[128], W3 [128 x 6], b3[6]. */
+#define EB_WS_NIN 48
+#define EB_WS_NOUT 6
+#define EB_WS_NPARAMS 23558
+/* Standalone network kernels on host arrays (each call uploads, runs, downloads).
+ * Loss = mean over rows and outputs of (y - T)^2; rows whose target is NaN add nothing. */
+int eb_mlp_forward(const float *params, const float *X /* n x 48 */, int64_t n, float *Y /* n x 6 */);
+int eb_mlp_loss_grad(const float *params, const float *X, const float *T /* n x 6 */, int64_t n, double *loss,
+                     float *grad /* EB_WS_NPARAMS */);
+/* Adam (0.9, 0.999, 1e-8) on shuffled minibatches (seeded order); params in/out. */
+int eb_mlp_train(float *params, const float *X, const float *T, int64_t n, int32_t epochs, int32_t batch, float lr,
+                 uint64_t seed, double *loss_per_epoch /* epochs, may be NULL */);
+/* The network a batch uses when eb_params.warm_start = EB_WS_LEARNED, with its
+ * normalisation: x = (f - in_shift) / in_scale over the EB_WS_NRAW raw features
+ * f (inputs beyond them are 0), and for the 3 translations and 3 rotations of
+ * node i:  ΔD_i = Δt Ḋ_i + Δt²/2 D̈_i + Δt² out_scale ⊙ y_i.  params NULL removes it. */
+#define EB_WS_NRAW 39
+int eb_ws_set_model(eb_handle *h, const float *params, const float *in_shift /* 48 */, const float *in_scale /* 48 */,
+                    const float *out_scale /* 6 */);
+/* Training-sample capture from the running solver: after each eb_step, eb_commit
+ * stores for every node with (node + commits) % stride == 0 its raw features at
+ * the step's start and the raw target (converged increment - Δt Ḋ - Δt²/2 D̈) / Δt²
+ * (NaN for simulations outside the commit mask) in a device ring of `capacity`
+ * samples.  capacity 0 stops capturing and frees the ring. */
+int eb_ws_capture(eb_handle *h, int64_t capacity, int32_t stride);
+/* Copies ring slots [first, first + n) to the host; *written = slots filled so far (<= capacity). */
+int eb_ws_samples(eb_handle *h, int64_t first, int64_t n, float *features /* n x 39 */, float *targets /* n x 6 */,
+                  int64_t *written);
 
 #ifdef __cplusplus
 }
