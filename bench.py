@@ -1,16 +1,27 @@
 #!/usr/bin/env python3
-"""Benchmark of the batched GB300 hot path: whole-job HHT steps/s.
+"""Benchmark of the batched GB300 hot path: whole-job HHT steps/s and Newton iterations/step.
 
 One "step" is one HHT step (predictor + Newton corrector with GMRES solves)
 of every simulation of the workload, through the library's C ABI.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
 Workloads (synthetic, seeded; no dataset):
-  nets256 — configuration 2: 256 square nets, sides U{20..40} (seed 0), 1 mm
-            spacing, xy jitter U(±0.5 mm), r = 0.1 mm, E = 100 GPa, gravity,
-            dropped on a sphere R = 15 mm given as a 128³ SDF at 0.3 mm; μ = 0.2,
-            Δt = 5e-5 s.
+  stents1024 (default) — 1024 braided stents drawn with seed 2: wires in
+            {16,24,32,48}, radius U[3,5] mm, pitch U[35,55] deg, elements per
+            wire U{100..400}, length ~20 mm, crossings merged, r = 0.05 mm,
+            E = 50 GPa, each released stress free into its own cylinder SDF
+            (radius U[0.85,0.95] of the stent's, 0.1 mm grid sized to the stent);
+            mu = 0.1, dt = 1e-5 s, FP32 GMRES inside FP64 refinement.  The
+            population runs as resident groups sized to the device memory;
+            the learned warm start (committed model) is on.  The line also
+            carries the same first group with the plain HHT predictor and the
+            plain single-stent path (48 wires, R = 4 mm, 45 deg, 200 elements
+            per wire, cylinder 3.5 mm) on the same GPU.
+  stent   — the single 48-wire stent above.
+  nets256 — 256 square nets, sides U{20..40} (seed 0), 1 mm spacing, xy jitter
+            U(±0.5 mm), r = 0.1 mm, E = 100 GPa, gravity, dropped on a sphere
+            R = 15 mm given as a 128³ SDF at 0.3 mm; mu = 0.2, dt = 5e-5 s.
 
 Under torchrun (N > 1) every rank runs its own full copy of the workload on
 its GPU (weak scaling; simulations are independent, no collective in the
@@ -39,48 +50,144 @@ sys.path.insert(0, ROOT)
 # k_beam (profiles/beam_kernel_nets16.md).
 F_ELEM_FP64 = 1998.0
 
+METRIC = "HHT steps/s & Newton iters/step, batched+learned vs plain"
+MODEL = os.path.join(ROOT, "endobeams.jl_gb300", "models", "warm_start_stents.npz")
+STENT_TOL_RES = 1e-7   # FP64 floor of the normalised residual reaches 1.4e-8 on the largest stents
+STENT_TOL_DISP = 1e-8
+
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="nets256")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="stents1024")
+    ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
+    ap.add_argument("--warm-start", default=None, choices=[None, "off", "learned"])
+    ap.add_argument("--count", type=int, default=None, help="population size override (stents)")
+    ap.add_argument("--mem-frac", type=float, default=0.75, help="device memory fraction per resident group")
     ap.add_argument("--cpu-sample", type=int, default=2, help="simulations in the CPU-baseline sample")
-    ap.add_argument("--cpu-steps", type=int, default=10, help="steps per simulation in the CPU-baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="steps per simulation in the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-batch and single-stent legs")
     return ap.parse_args()
 
 
-# ------------------------------------------------------------------ workload
+# ------------------------------------------------------------------ workloads
 
-def build_workload(name: str, precision: str = "fp64", rank: int = 0):
+def _pkg():
     import __graft_entry__ as g
-    g.load_package()
-    from endobeams_gb300 import scenes
-    if name in ("nets256", "nets16"):
-        count = 256 if name == "nets256" else 16
-        sides = scenes.net_sides(256, seed=0)[:count]
-        sdf = scenes.sphere_sdf()
-        confs, inters = [], []
-        params = None
-        for i, side in enumerate(sides):
-            c, p, it = scenes.net_on_sphere(int(side), seed=1 + i, sdf=sdf)
-            confs.append(c)
-            inters.append(it)
-            params = p
-        params.tolerance_residual = 1e-5
-        params.tolerance_displacement = 1e-8
-        params.precision = precision
-        desc = {"workload": f"{name}: {count} nets (sides U{{20..40}}) on a 128^3 sphere SDF, dt=5e-5",
-                "sims": count, "nodes": int(sum(len(c.nodes) for c in confs)),
-                "elements": int(sum(len(c.beams) for c in confs)),
-                "tolerance_residual": 1e-5, "tolerance_displacement": 1e-8, "precision": precision}
-        return confs, params, inters, desc
-    raise SystemExit(f"unknown workload {name}")
+    return g.load_package()
+
+
+def stent_params(p, precision="mixed", warm="off"):
+    p.tolerance_residual = STENT_TOL_RES
+    p.tolerance_displacement = STENT_TOL_DISP
+    p.krylov_restart = 32
+    p.precision = precision
+    p.warm_start = warm
+    return p
+
+
+class Workload:
+    """A named workload: simulations built lazily in resident groups."""
+
+    def __init__(self, name, precision=None, warm=None, count=None):
+        _pkg()
+        from endobeams_gb300 import scenes
+        self.scenes = scenes
+        self.name = name
+        self.kind = "stents" if name.startswith("stent") else "nets"
+        if self.kind == "nets":
+            if name not in ("nets256", "nets16"):
+                raise SystemExit(f"unknown workload {name}")
+            self.count = 256 if name == "nets256" else 16
+            self.sides = scenes.net_sides(256, seed=0)[:self.count]
+            self.precision = precision or "fp64"
+            self.warm = "off"
+            self.sdf = None
+        else:
+            if name == "stent":
+                self.variants = [None]
+            elif name.startswith("stents"):
+                n = count or int(name[len("stents"):] or 1024)
+                self.variants = scenes.stent_variants(1024, seed=2)[:n]
+            else:
+                raise SystemExit(f"unknown workload {name}")
+            self.count = len(self.variants)
+            self.precision = precision or "mixed"
+            self.warm = warm or ("learned" if (name != "stent" and os.path.exists(MODEL)) else "off")
+
+    def stats(self, i):
+        """(nodes, elements, RCM half bandwidth in nodes, SDF points, Krylov restart) of simulation i (cached)."""
+        if not hasattr(self, "_stats"):
+            self._stats = {}
+        if i not in self._stats:
+            from endobeams_gb300 import _lib
+            c, p, it = self.build(i)
+            _, w = _lib.rcm_order(len(c.nodes), c.beams.conn)
+            m = getattr(it, "master", None) if it is not None else None
+            pts = (m.dims[0] + 2) * (m.dims[1] + 2) * (m.dims[2] + 2) if m is not None and hasattr(m, "dims") else 0
+            self._stats[i] = (len(c.nodes), len(c.beams), w, pts, p.krylov_restart)
+        return self._stats[i]
+
+    def build(self, i):
+        s = self.scenes
+        if self.kind == "nets":
+            if self.sdf is None:
+                self.sdf = s.sphere_sdf()
+            c, p, it = s.net_on_sphere(int(self.sides[i]), seed=1 + i, sdf=self.sdf)
+            p.tolerance_residual = 1e-5
+            p.tolerance_displacement = 1e-8
+            p.precision = self.precision
+            return c, p, it
+        v = self.variants[i]
+        c, p, it = s.braided_stent() if v is None else s.stent_variant(v)
+        return c, stent_params(p, self.precision, self.warm), it
+
+    def describe(self, nodes, elements, groups):
+        if self.kind == "nets":
+            w = f"{self.name}: {self.count} nets (sides U{{20..40}}) on a 128^3 sphere SDF, dt=5e-5"
+            tol = (1e-5, 1e-8)
+        elif self.name == "stent":
+            w = "stent: one braided stent (48 wires, R 4 mm, 45 deg, 200 elements/wire) in a 3.5 mm cylinder SDF, dt=1e-5"
+            tol = (STENT_TOL_RES, STENT_TOL_DISP)
+        else:
+            w = (f"{self.name}: {self.count} braided stents (seed 2; wires {{16,24,32,48}}, R U[3,5] mm, pitch "
+                 f"U[35,55] deg, U{{100..400}} elements/wire, own cylinder SDF at 0.1 mm), dt=1e-5")
+            tol = (STENT_TOL_RES, STENT_TOL_DISP)
+        return {"workload": w, "sims": self.count, "nodes": int(nodes), "elements": int(elements),
+                "resident_groups": groups, "tolerance_residual": tol[0], "tolerance_displacement": tol[1],
+                "precision": self.precision, "warm_start": self.warm}
+
+
+def est_bytes(stats):
+    """Device bytes eb_create will hold for one simulation (layout of eb_internal.cuh):
+    element staging, six FP64 BSR matrices plus the FP32 tangent, node state, DOF vectors,
+    Krylov basis, FP32 band and its diagonal-block inverses, SDF coefficients."""
+    n, ne, w, pts, m = stats
+    b = 6 * w + 5
+    blocks = n + 2 * ne
+    band = 4 * (6 * n) * (2 * b + 1) if b <= 892 else 0
+    per_dof = 14 * 8 + 1 + 16 + (m + 1) * 8 + 8 + 4 + 256
+    return 6300 * ne + 2200 * blocks + 1100 * n + per_dof * 6 * n + band + 8 * pts
+
+
+def plan_groups(wl, budget):
+    """Greedy resident groups in population order under a device-byte budget."""
+    groups, cur, acc = [], [], 0
+    for i in range(wl.count):
+        bts = est_bytes(wl.stats(i))
+        if cur and acc + bts > budget:
+            groups.append(cur)
+            cur, acc = [], 0
+        cur.append(i)
+        acc += bts
+    if cur:
+        groups.append(cur)
+    return groups
 
 
 # ------------------------------------------------------------------ clocks
@@ -138,7 +245,7 @@ class ClockSampler:
 # ------------------------------------------------------------------ GPU arm
 
 class Driver:
-    """The batched time loop of run_simulation! at fixed Δt (the workload's Δt is its maximum)."""
+    """The batched time loop of run_simulation! (per-simulation Δt halving and rollback)."""
 
     def __init__(self, eng, params):
         self.eng = eng
@@ -146,10 +253,15 @@ class Driver:
         self.S = eng.n
         self.t = np.zeros(self.S)
         self.dt = np.full(self.S, params.initial_timestep)
+        self.reset()
+
+    def reset(self):
         self.ok_steps = 0
         self.newton = 0
         self.krylov = 0
         self.batch_iters = 0
+        self.ws_used = 0
+        self.ws_steps = 0
 
     def step(self, e2e=False, ubuf=None):
         eng = self.eng
@@ -160,6 +272,8 @@ class Driver:
         self.newton += sum(s["newton_iterations"] for s in st)
         self.batch_iters += max(s["newton_iterations"] for s in st)
         self.krylov += sum(s["krylov_iterations"] for s in st)
+        self.ws_used += sum(s["warm_start_used"] for s in st)
+        self.ws_steps += len(st)
         failed = k > self.p.max_iterations
         ok = ~failed
         if failed.any():
@@ -173,81 +287,179 @@ class Driver:
         return k
 
 
-def gpu_arm(args, rank, world):
-    import __graft_entry__ as g
-    eb = g.load_package()
-    from endobeams_gb300 import _lib
-    confs, params, inters, desc = build_workload(args.workload, args.precision, rank)
+def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
+    """Creates one resident group, warms up, times args.steps steps; returns a dict of totals."""
+    built = [wl.build(i) for i in idx]
+    confs = [b[0] for b in built]
+    inters = [b[2] for b in built]
+    params = built[0][1]
+    if warm is not None:
+        params.warm_start = warm
     params.timing = True
-    n_gpu, gname = eb.device_info()
-    if n_gpu < 1:
-        raise SystemExit("no CUDA device")
     eng = eb.GpuSimulations(confs, params, inters)
+    if params.warm_start == "learned":
+        from endobeams_gb300 import warm_start as W
+        eng.set_warm_start(W.WarmStartModel.load(MODEL))
+    mem, band_sims = eng.memory()
     drv = Driver(eng, params)
     for _ in range(args.warmup):
         drv.step()
     eng.phase_times(reset=True)
-    drv.ok_steps = drv.newton = drv.krylov = 0
+    drv.reset()
     barrier(world)
-    clocks = ClockSampler()
-    clocks.start()
     eng.timer_start()
     for _ in range(args.steps):
         drv.step()
-    ms = eng.timer_stop()
-    clk = clocks.stop()
-    ms = allreduce_max(ms, world)
+    ms = allreduce_max(eng.timer_stop(), world)
     phase_ms, launches = eng.phase_times(reset=True)
-    sim_steps = drv.ok_steps
-    newton_per_step = drv.newton / max(sim_steps, 1)
-    krylov_per_newton = drv.krylov / max(drv.newton, 1)
-    value = world * sim_steps / (ms / 1e3)
-    # ---- end to end through the public API with host buffers
-    e2e = None
-    if not args.no_e2e:
-        total_nodes = desc["nodes"]
+    out = {"sim_steps": drv.ok_steps, "ms": ms, "newton": drv.newton, "krylov": drv.krylov,
+           "ws_used": drv.ws_used, "ws_steps": drv.ws_steps, "phase_ms": phase_ms, "launches": launches,
+           "nodes": sum(len(c.nodes) for c in confs), "elements": sum(len(c.beams) for c in confs),
+           "sims": len(idx), "device_bytes": mem, "band_sims": band_sims, "e2e": None}
+    if e2e and not args.no_e2e:
+        total_nodes = out["nodes"]
         ubuf = np.zeros((total_nodes, 3))
         n_loaded = sum(len(c.loads.concentrated_force.loaded_dofs) for c in confs if c.loads is not None)
-        drv.ok_steps = drv.newton = drv.batch_iters = 0
+        drv.reset()
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             drv.step(e2e=True, ubuf=ubuf)
         wall = allreduce_max(time.perf_counter() - t0, world)
         S = drv.S
-        bi = drv.batch_iters / max(args.steps, 1)  # batched Newton iterations per step
+        bi = drv.batch_iters / max(args.steps, 1)
         # loads, per-sim step constants (cK, cC, cM, dt), active masks (step + each iteration), commit mask
         h2d = 8 * n_loaded + 32 * S + 4 * S + 4 * S * bi + 4 * S
         # displacements, per-iteration Newton norms, per-step solver statistics
-        d2h = 24 * total_nodes + 32 * S * bi + 20 * S
-        e2e = {"value": world * drv.ok_steps / wall, "unit": "HHT steps/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
-    # ---- roofline of the dominant kernel
-    peak_fp64 = eb.fp64_peak_tflops()
+        d2h = 24 * total_nodes + 40 * S * bi + 20 * S
+        out["e2e"] = {"sim_steps": drv.ok_steps, "wall_s": wall, "h2d": h2d, "d2h": d2h}
+    eng.close()
+    return out
+
+
+def gmres_bytes_per_iter(wl, idx):
+    """Algorithmic bytes one GMRES iteration reads per simulation (FP32 band L and U, the
+    32x32 diagonal-block inverses, the FP32 tangent and its block index), summed over idx."""
+    tot = 0
+    for i in idx:
+        n, ne, w, _, _ = wl.stats(i)
+        b = 6 * w + 5
+        N = 6 * n
+        tot += 4 * N * (2 * b + 1) + 2 * 4 * 32 * N + (n + 2 * ne) * (36 * 4 + 4)
+    return tot
+
+
+def gpu_arm(args, rank, world):
+    eb = _pkg()
+    from endobeams_gb300 import _lib
+    wl = Workload(args.workload, args.precision, args.warm_start, args.count)
+    n_gpu, gname = eb.device_info()
+    if n_gpu < 1:
+        raise SystemExit("no CUDA device")
+    free, total = _lib.device_memory()
+    groups = plan_groups(wl, int(args.mem_frac * free)) if wl.kind == "stents" else [list(range(wl.count))]
+    clocks = ClockSampler()
+    clocks.start()
+    tot = None
+    for g_idx in groups:
+        r = run_group(eb, wl, g_idx, args, world)
+        if tot is None:
+            tot = r
+            tot["e2e"] = dict(r["e2e"]) if r["e2e"] else None
+            tot["phase_ms"] = dict(r["phase_ms"])
+            tot["launches"] = dict(r["launches"])
+            tot["device_bytes_max"] = r["device_bytes"]
+        else:
+            for k in ("sim_steps", "ms", "newton", "krylov", "ws_used", "ws_steps", "nodes", "elements", "sims",
+                      "band_sims"):
+                tot[k] += r[k]
+            tot["device_bytes_max"] = max(tot["device_bytes_max"], r["device_bytes"])
+            for k in tot["phase_ms"]:
+                tot["phase_ms"][k] += r["phase_ms"][k]
+                tot["launches"][k] += r["launches"][k]
+            if tot["e2e"] and r["e2e"]:
+                for k in ("sim_steps", "wall_s", "h2d", "d2h"):
+                    tot["e2e"][k] += r["e2e"][k]
+    clk = clocks.stop()
+    value = world * tot["sim_steps"] / (tot["ms"] / 1e3)
+    steps = args.steps
+    e2e = None
+    if tot["e2e"]:
+        e = tot["e2e"]
+        e2e = {"value": world * e["sim_steps"] / e["wall_s"], "unit": "HHT steps/s",
+               "h2d_bytes_per_step": int(e["h2d"] / max(steps, 1)), "d2h_bytes_per_step": int(e["d2h"] / max(steps, 1))}
+    phase_ms, launches = tot["phase_ms"], tot["launches"]
     dom = max(phase_ms, key=lambda k: phase_ms[k])
-    roof = None
-    beam_launches = launches["beam"]
-    if beam_launches:
-        avg_beam_ms = phase_ms["beam"] / beam_launches
-        flops = (F_ELEM_FP64 or float("nan")) * desc["elements"]
-        achieved = flops / (avg_beam_ms * 1e-3) / 1e12
-        roof = {"kernel": "k_beam (corotational element, FP64)", "bound": "fp64", "achieved": achieved,
-                "peak": peak_fp64, "peak_source": "measured (eb_fp64_peak FMA probe on this GPU)",
-                "unit": "TFLOP/s", "frac": achieved / peak_fp64, "traffic": None,
-                "avg_launch_ms": avg_beam_ms, "share_of_step": phase_ms["beam"] / sum(phase_ms.values())}
+    # ---- rooflines: the element kernel (FP64 pipe) and the Krylov kernel (HBM)
+    peak_fp64 = eb.fp64_peak_tflops()
+    rooflines = {}
+    if launches["beam"]:
+        avg_beam_ms = phase_ms["beam"] / launches["beam"]
+        ach = F_ELEM_FP64 * tot["elements"] / len(groups) / (avg_beam_ms * 1e-3) / 1e12
+        rooflines["beam"] = {"kernel": "k_beam (corotational element, FP64)", "bound": "fp64", "achieved": ach,
+                             "peak": peak_fp64, "peak_source": "measured (eb_fp64_peak FMA probe on this GPU)",
+                             "unit": "TFLOP/s", "frac": ach / peak_fp64, "traffic": None,
+                             "avg_launch_ms": avg_beam_ms, "share_of_step": phase_ms["beam"] / sum(phase_ms.values())}
+    peaks = _measured_peaks()
+    if launches["krylov"] and wl.kind == "stents":
+        per_iter = gmres_bytes_per_iter(wl, range(wl.count))
+        iters_per_sim = tot["krylov"] / max(tot["sims"], 1)  # summed over the timed steps
+        bytes_total = per_iter * iters_per_sim
+        ach = bytes_total / (phase_ms["krylov"] * 1e-3) / 1e9
+        hbm = peaks.get("hbm_gbs")
+        rooflines["krylov"] = {"kernel": "k_gmres (per-simulation restarted GMRES, band-LU preconditioned)",
+                               "bound": "hbm", "achieved": ach, "peak": hbm,
+                               "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else None, "unit": "GB/s",
+                               "frac": (ach / hbm) if hbm else None, "traffic": None,
+                               "algorithmic_bytes_per_iteration": per_iter / max(wl.count, 1),
+                               "share_of_step": phase_ms["krylov"] / sum(phase_ms.values())}
+    roof = rooflines.get("krylov") if dom in ("krylov", "precond") and "krylov" in rooflines else rooflines.get("beam")
     out = {
-        "metric": "HHT steps/s (whole job), batched plain Newton",
-        "value": value, "unit": "HHT steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f64+f32-krylov", "data": "synthetic",
-        "config": dict(desc, l2="state and staging arrays exceed L2 (129 MB) each step", device=gname),
-        "newton_iters_per_step": newton_per_step, "krylov_iters_per_newton": krylov_per_newton,
+        "metric": METRIC if wl.kind == "stents" else "HHT steps/s (whole job), batched plain Newton",
+        "value": value, "unit": "HHT steps/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": tot["ms"] / len(groups) / max(steps, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if wl.precision == "fp64" else "f64+f32-krylov", "data": "synthetic",
+        "config": dict(wl.describe(tot["nodes"], tot["elements"], len(groups)),
+                       l2="state, band and staging arrays exceed L2 (129 MB) each step", device=gname,
+                       device_bytes_per_group_max=int(tot["device_bytes_max"]), band_preconditioned_sims=tot["band_sims"]),
+        "newton_iters_per_step": tot["newton"] / max(tot["sim_steps"], 1),
+        "krylov_iters_per_newton": tot["krylov"] / max(tot["newton"], 1),
         "phase_ms": {k: round(v, 3) for k, v in phase_ms.items()}, "dominant_phase": dom,
         "gpu_launches": int(sum(launches.values())),
-        "roofline": roof, "e2e": e2e, "clocks": clk,
+        "roofline": roof, "rooflines": rooflines, "e2e": e2e, "clocks": clk,
     }
-    eng.close()
-    return out, confs, params, inters, desc
+    if wl.warm == "learned":
+        out["warm_start"] = {"model": os.path.relpath(MODEL, ROOT),
+                             "learned_start_accepted_frac": tot["ws_used"] / max(tot["ws_steps"], 1)}
+    # ---- comparison legs: the first group with the plain predictor, and the plain single stent
+    if wl.kind == "stents" and wl.count > 1 and not args.no_compare:
+        if wl.warm == "learned":
+            r = run_group(eb, wl, groups[0], args, world, e2e=False, warm="off")
+            out["batched_plain"] = {"value": world * r["sim_steps"] / (r["ms"] / 1e3), "sims": r["sims"],
+                                    "newton_iters_per_step": r["newton"] / max(r["sim_steps"], 1),
+                                    "note": "first resident group, HHT predictor"}
+        single = Workload("stent", wl.precision, "off")
+        r = run_group(eb, single, [0], args, world, e2e=False)
+        sv = world * r["sim_steps"] / (r["ms"] / 1e3)
+        out["plain_single_sim"] = {"value": sv, "unit": "HHT steps/s",
+                                   "newton_iters_per_step": r["newton"] / max(r["sim_steps"], 1),
+                                   "workload": single.describe(r["nodes"], r["elements"], 1)["workload"]}
+        out["speedup_vs_plain_single_sim"] = value / sv
+    return out, wl
+
+
+def _measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+    except Exception:
+        return {}
+    out = {}
+    for k, v in d.items():
+        if isinstance(v, (int, float)):
+            out[k] = float(v)
+    return out
 
 
 # ------------------------------------------------------------------ CPU arms (oracle restatement)
@@ -274,8 +486,11 @@ def _timed_chunk(payload):
     import __graft_entry__ as g
     O = g.load_oracle()
     import bridge
-    confs, params, inters, _ = build_workload(workload, precision)
-    models = [O.OracleModel(bridge.scene_from_conf(confs[i], inters[i]), bridge.params_from(params)) for i in idx]
+    wl = Workload(workload, precision, "off")
+    models = []
+    for i in idx:
+        c, p, it = wl.build(i % wl.count)
+        models.append(O.OracleModel(bridge.scene_from_conf(c, it), bridge.params_from(p)))
     t0 = time.perf_counter()
     done = 0
     for m in models:
@@ -318,25 +533,25 @@ def main():
         if rank != 0:
             return
         cores = os.cpu_count() or 1
+        wl = Workload(args.workload, args.precision, "off", args.count)
         sample = max(args.cpu_sample, cores)
-        rate, wall = cpu_rate(args.workload, args.precision, sample, args.cpu_steps, cores)
-        _, _, _, desc = build_workload(args.workload, args.precision)
-        line = {"metric": "HHT steps/s (whole job), batched plain Newton", "impl": "reference", "value": rate,
-                "unit": "HHT steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": desc,
+        rate, wall = cpu_rate(args.workload, wl.precision, sample, args.cpu_steps, cores)
+        line = {"metric": METRIC if wl.kind == "stents" else "HHT steps/s (whole job), batched plain Newton",
+                "impl": "reference", "value": rate, "unit": "HHT steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": {"workload": wl.name, "sims": wl.count},
                 "cpu_baseline": {"value": rate, "unit": "HHT steps/s", "cores": cores, "kind": "port",
-                                 "sample": f"{sample} of {desc['sims']} sims x {args.cpu_steps} steps, "
+                                 "sample": f"{sample} of {wl.count} sims x {args.cpu_steps} steps, "
                                            f"C++ oracle + SciPy SuperLU, {cores} processes, {wall:.1f} s"},
                 "e2e": {"value": rate, "unit": "HHT steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
-    out, confs, params, inters, desc = gpu_arm(args, rank, world)
+    out, wl = gpu_arm(args, rank, world)
     if rank == 0:
         if not args.no_cpu:
-            rate, wall = cpu_rate(args.workload, args.precision, args.cpu_sample, args.cpu_steps, 1)
+            rate, wall = cpu_rate(args.workload, wl.precision, args.cpu_sample, args.cpu_steps, 1)
             out["cpu_baseline"] = {"value": rate, "unit": "HHT steps/s", "cores": 1, "kind": "port",
-                                   "sample": f"{args.cpu_sample} of {desc['sims']} sims x {args.cpu_steps} steps, "
+                                   "sample": f"{args.cpu_sample} of {wl.count} sims x {args.cpu_steps} steps, "
                                              f"C++ oracle + SciPy SuperLU, 1 core, {wall:.1f} s"}
         print(json.dumps(out))
 

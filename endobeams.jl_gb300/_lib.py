@@ -86,6 +86,7 @@ SIGNATURES = {
     "eb_contact_eval": (C.c_int, [C.c_int64, P_d, P_d, P_d, P_d, P_d, P_d, P_i32]),
     "eb_device_info": (C.c_int, [P_i32, C.c_char_p, C.c_int32]),
     "eb_rcm_order": (C.c_int, [C.c_int64, P_i64, P_i32, P_i32, P_i32]),
+    "eb_device_memory": (C.c_int, [P_i64, P_i64]),
     "eb_mlp_forward": (C.c_int, [P_f, P_f, C.c_int64, P_f]),
     "eb_mlp_loss_grad": (C.c_int, [P_f, P_f, P_f, C.c_int64, P_d, P_f]),
     "eb_mlp_train": (C.c_int, [P_f, P_f, P_f, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P_d]),
@@ -159,6 +160,31 @@ def device_info():
     name = C.create_string_buffer(256)
     rc = L.eb_device_info(C.byref(n), name, 256)
     return (n.value, name.value.decode()) if rc == EB_OK else (0, "")
+
+
+def device_memory():
+    """(free, total) bytes of the current device."""
+    f, t = C.c_int64(0), C.c_int64(0)
+    check(load().eb_device_memory(C.byref(f), C.byref(t)), "eb_device_memory")
+    return int(f.value), int(t.value)
+
+
+def rcm_order(n: int, edges: np.ndarray):
+    """(positions, half bandwidth) of the band preconditioner's reverse Cuthill-McKee order
+    of an n-node graph given as an (m, 2) array of 0-based edges."""
+    e = np.asarray(edges, np.int64).reshape(-1, 2)
+    src = np.concatenate([e[:, 0], e[:, 1]])
+    dst = np.concatenate([e[:, 1], e[:, 0]]).astype(np.int32)
+    order = np.argsort(src, kind="stable")
+    adjncy = np.ascontiguousarray(dst[order])
+    xadj = np.zeros(n + 1, np.int64)
+    np.add.at(xadj, src + 1, 1)
+    xadj = np.cumsum(xadj)
+    pos = np.zeros(n, np.int32)
+    bw = C.c_int32(0)
+    check(load().eb_rcm_order(n, ptr(xadj, C.c_int64), ptr(adjncy, C.c_int32), ptr(pos, C.c_int32), C.byref(bw)),
+          "eb_rcm_order")
+    return pos, int(bw.value)
 
 
 def default_params() -> EbParams:

@@ -259,7 +259,8 @@ class SimulationParams:
     timing: bool = False             # per-phase CUDA-event timing inside each step
     preconditioner: str = "band"     # "band" (FP32 band LU, RCM order) | "block_jacobi"
     refactor_its: int = 16           # reuse the band LU until a solve needs more GMRES iterations (0: always refactor)
-    stage_band: bool = True          # stream band blocks into shared memory with bulk async copies
+    stage_band: int = 1              # 1: stream band blocks into shared memory with bulk async copies; 0: off;
+                                     # 2: test of the bounded wait (the first block's wait runs out)
     warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start)
 
     def to_c(self) -> _lib.EbParams:
@@ -280,7 +281,7 @@ class SimulationParams:
         p.timing = 1 if self.timing else 0
         p.preconditioner = 1 if self.preconditioner == "block_jacobi" else 0
         p.refactor_its = int(self.refactor_its)
-        p.stage_band = int(bool(self.stage_band))
+        p.stage_band = int(self.stage_band)
         if self.warm_start not in ("off", "learned"):
             raise ValueError("warm_start must be 'off' or 'learned'")
         p.warm_start = 1 if self.warm_start == "learned" else 0

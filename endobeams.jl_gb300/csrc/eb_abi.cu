@@ -442,6 +442,15 @@ int eb_rcm_order(int64_t n, const int64_t* xadj, const int32_t* adjncy, int32_t*
   return EB_OK;
 }
 
+int eb_device_memory(int64_t* free_bytes, int64_t* total_bytes) {
+  size_t fr = 0, tot = 0;
+  cudaError_t e = cudaMemGetInfo(&fr, &tot);
+  if (e != cudaSuccess) return fail(EB_ERR_CUDA, "cudaMemGetInfo: %s", cudaGetErrorString(e));
+  if (free_bytes) *free_bytes = (int64_t)fr;
+  if (total_bytes) *total_bytes = (int64_t)tot;
+  return EB_OK;
+}
+
 int eb_device_info(int32_t* count, char* name, int32_t name_len) {
   int c = 0;
   cudaError_t e = cudaGetDeviceCount(&c);
@@ -877,7 +886,14 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     CK(A.alloc(&p_li, inv));
     CK(A.alloc(&p_ui, inv));
     CK(A.alloc(&h->d_refactor, n_sims));
-    h->band = BandDev{p_band, p_boff, p_bw, p_pos, p_nat, p_work, p_li, p_ui, h->d_refactor};
+    // CTA order of the per-simulation kernels: decreasing n (b + 1) (band solve and LU work)
+    std::vector<int> order(n_sims);
+    for (int s = 0; s < n_sims; ++s) order[s] = s;
+    auto cost = [&](int s) { return (h->node_off[s + 1] - h->node_off[s]) * (int64_t)(h->band_b[s] + 6); };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    int* p_order;
+    CK(A.upload(&p_order, order));
+    h->band = BandDev{p_band, p_boff, p_bw, p_pos, p_nat, p_work, p_li, p_ui, h->d_refactor, p_order};
     sa.band = h->band;
     h->need_refactor.assign(n_sims, 1);
     h->refactor_mask.assign(n_sims, 0);
@@ -890,6 +906,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     sa.x_in_smem = h->any_band && gmres_smem(m) + sizeof(float) * (size_t)max_n <= 200 * 1024;
     // stage band blocks through shared memory when the two buffers fit beside the rest
     sa.stage_floats = 0;
+    sa.stage_test_extra = p->stage_band == 2 ? 16 : 0;
     if (h->any_band && p->stage_band) {
       sa.stage_floats = kPanel * (h->max_b + 1);
       if (gmres_smem_total(sa) > kGmresSmemLimit) sa.stage_floats = 0;
@@ -1182,6 +1199,14 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     for (int s = 0; s < S; ++s) {
       if (!running[s]) continue;
       const double* q = &h->h_norms[5 * s];
+      if (q[4] < 0) {
+        // a bulk-copy wait ran out in this solve: stop this simulation's Newton loop (the step
+        // reports EB_SIM_WAIT_TIMEOUT) and read band blocks from global memory from now on
+        h->sa.stage_floats = 0;
+        running[s] = 0;
+        k[s] = P.max_iterations + 1;
+        continue;
+      }
       if (h->P.refactor_its > 0 && q[4] > h->P.refactor_its) h->need_refactor[s] = 1;
       // compute_norms_corrector (utils_solver.jl:126-151)
       double dnorm = std::sqrt(q[0]);

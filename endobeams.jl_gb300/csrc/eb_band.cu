@@ -47,7 +47,7 @@ void launch_band_fill(const Dev& d, const BandDev& B, const int* blk_row, cudaSt
 constexpr int kLuThreads = 256;
 
 __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
-  const int s = blockIdx.x;
+  const int s = B.order[blockIdx.x];
   if (!d.active[s] || !B.refactor[s]) return;
   const int b = B.bw[s];
   if (b == 0) return;
@@ -134,32 +134,34 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
       for (int r = 0; r < kPanel; ++r) Uv[lane * kPanel + r] = z[r];
     }
     __syncthreads();
-    // ---- 3. trailing update on 4x4 tiles
-    const int tq = (q + 3) >> 2;
-    for (int tile = threadIdx.x; tile < tq * tq; tile += kLuThreads) {
-      const int ti = tile % tq, tj = tile / tq;
-      const int i0 = ti * 4, j0 = tj * 4;
-      float acc[4][4];
+    // ---- 3. trailing update A22 -= L21 U12 on 8x8 register tiles with strided rows and
+    // columns (thread (ti, tj) owns rows ti + a R and columns tj + c R, R = ceil(q / 8)):
+    // consecutive lanes read consecutive panel rows (no bank conflicts), share the U12
+    // row (broadcast) and update consecutive band entries (coalesced).
+    const int R = (q + 7) >> 3;
+    for (int tile = threadIdx.x; tile < R * R; tile += kLuThreads) {
+      const int ti = tile % R, tj = tile / R;
+      float acc[8][8];
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+      for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[a][c] = 0.f;
+        for (int c = 0; c < 8; ++c) acc[a][c] = 0.f;
       for (int t = 0; t < kb; ++t) {
-        float l[4], u[4];
+        float l[8], u[8];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) l[a] = (i0 + a < q) ? P[(kb + i0 + a) + ldp * t] : 0.f;
+        for (int a = 0; a < 8; ++a) l[a] = (ti + a * R < q) ? P[(kb + ti + a * R) + ldp * t] : 0.f;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) u[c] = (j0 + c < q) ? U[t * b + j0 + c] : 0.f;
+        for (int c = 0; c < 8; ++c) u[c] = (tj + c * R < q) ? U[t * b + tj + c * R] : 0.f;
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+        for (int a = 0; a < 8; ++a)
 #pragma unroll
-          for (int c = 0; c < 4; ++c) acc[a][c] += l[a] * u[c];
+          for (int c = 0; c < 8; ++c) acc[a][c] = fmaf(l[a], u[c], acc[a][c]);
       }
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
+      for (int c = 0; c < 8; ++c)
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
-          if (i0 + a < q && j0 + c < q) V.at(k0 + kb + i0 + a, k0 + kb + j0 + c) -= acc[a][c];
+        for (int a = 0; a < 8; ++a)
+          if (ti + a * R < q && tj + c * R < q) V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) -= acc[a][c];
     }
     // ---- write back panel and U12
     if (lane < kb)

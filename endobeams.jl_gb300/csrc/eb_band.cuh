@@ -31,6 +31,8 @@ struct BandDev {
   float* Linv;              // per panel: inverse of the unit-lower diagonal block (column-major)
   float* Uinv;              // per panel: inverse of the upper diagonal block (column-major)
   const int* refactor;      // per sim: 1 = refill and refactorise before this solve
+  const int* order;         // CTA b of the per-simulation kernels works on simulation order[b]
+                            // (largest first, so the last wave holds the smallest simulations)
 };
 
 constexpr int kPanel = 32;  // panel width of the blocked factorisation and solves
@@ -103,6 +105,7 @@ struct Stage {
   uint64_t* bar;    // two mbarriers
   int* fail;        // shared flag: a wait ran out (staging is then abandoned)
   int* pend;        // shared, thread 0 only: parity of the copy in flight per buffer, -1 none
+  uint32_t extra;   // bytes expected beyond the copies on the first block (timeout-path test; normally 0)
 };
 
 // Thread 0, at kernel end after a failed wait: waits (bounded) for copies still in flight.
@@ -145,7 +148,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     const uint32_t bytes = (uint32_t)(((int64_t)kb * colw * 4 + 15) & ~(int64_t)15);
     const float* isrc = (lower ? Li : Ui) + (int64_t)k0 * kPanel;
     fence_async_smem();
-    mbar_expect_tx(&st->bar[sb], bytes + 4096u);
+    mbar_expect_tx(&st->bar[sb], bytes + 4096u + (jb == 0 && lower ? st->extra : 0u));
     bulk_g2s(st->buf[sb], src, bytes, &st->bar[sb]);
     bulk_g2s(st->inv[sb], isrc, 4096u, &st->bar[sb]);
     st->pend[sb] = (int)ph[sb];

@@ -86,7 +86,7 @@ __device__ __forceinline__ void cta_prec(const TM* __restrict__ Dinv, int64_t n0
 
 template <typename T>
 __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
-  const int s = blockIdx.x;
+  const int s = a.band.order[blockIdx.x];
   if (!a.active[s]) return;
   const int m = a.m;
   const int64_t n0 = a.sim_node_off[s];
@@ -129,6 +129,7 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
     stage.bar = bars;
     stage.fail = &stage_fail;
     stage.pend = stage_pend;
+    stage.extra = (uint32_t)a.stage_test_extra;
     if (threadIdx.x == 0) {
       mbar_init(&bars[0], 1);
       mbar_init(&bars[1], 1);
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
     a.norms[5 * s + 1] = q[1];
     a.norms[5 * s + 2] = q[2];
     a.norms[5 * s + 3] = q[3];
-    a.norms[5 * s + 4] = (double)its;  // iterations of this solve
+    a.norms[5 * s + 4] = status == 4 ? -1.0 : (double)its;  // iterations of this solve (-1: a wait ran out)
     a.its[s] += its;
     a.refs[s] += refs;
     const double rel = bnorm > 0.0 ? rnorm / bnorm : 0.0;

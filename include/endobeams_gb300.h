@@ -78,7 +78,9 @@ typedef struct {
   int32_t refactor_its;                   /* band LU is reused until a solve needs more GMRES
                                              iterations than this or Δt changes (0: refactorise every solve) */
   int32_t stage_band;                     /* 1: the triangular solves stream band blocks into shared memory
-                                             with bulk asynchronous copies (same arithmetic, same results) */
+                                             with bulk asynchronous copies (same arithmetic, same results);
+                                             2: as 1, but the first block's wait expects 16 bytes that no copy
+                                             delivers, so it runs out (tests EB_SIM_WAIT_TIMEOUT) */
   int32_t warm_start;                     /* EB_WS_OFF | EB_WS_LEARNED (needs eb_ws_set_model) */
 } eb_params;
 
@@ -219,6 +221,8 @@ int eb_fp64_peak(double *tflops);
  * *half_bandwidth = max |pos[v] - pos[w]| over edges.  No reference counterpart
  * (the reference hands the matrix to PARDISO, src/linearsolvers.jl:15-23). */
 int eb_rcm_order(int64_t n, const int64_t *xadj, const int32_t *adjncy, int32_t *pos, int32_t *half_bandwidth);
+/* Free and total memory of the current device (bytes), for sizing batches before create. */
+int eb_device_memory(int64_t *free_bytes, int64_t *total_bytes);
 /* Device count and name probe (for hosts that must check before create). */
 int eb_device_info(int32_t *count, char *name, int32_t name_len);
 /* Selects the CUDA device for handles created afterwards on this thread (no

@@ -106,3 +106,24 @@ def test_staged_band_solve_bitwise(eb, scenes):
         out[staged] = (conf.nodes.un.copy(), res.krylov_iterations[0])
     assert np.array_equal(out[True][0], out[False][0])
     assert out[True][1] == out[False][1]
+
+
+def test_bulk_copy_wait_timeout_is_reported(eb, scenes):
+    """The shared-memory staging waits on mbarriers with an iteration limit.  With
+    stage_band = 2 the first block's wait expects bytes that no copy delivers: the
+    wait runs out, the step reports EB_SIM_WAIT_TIMEOUT as "not converged", the
+    context stays usable, and the next steps (staging switched off) converge."""
+    from endobeams_gb300 import _lib
+    conf, p, inter = scenes.net_on_sphere(24, steps=8, sdf=scenes.sphere_sdf(n=48, h=0.8e-3))
+    p.tolerance_residual = 1e-5
+    p.stage_band = 2
+    eng = eb.GpuSimulations([conf], p, [inter])
+    dt = np.full(1, p.initial_timestep)
+    k, status = eng.step(dt)
+    assert status[0] == 4 and k[0] > p.max_iterations
+    eng.rollback(np.ones(1, np.int32))
+    for _ in range(3):
+        k, status = eng.step(dt)
+        assert status[0] == 0 and k[0] <= p.max_iterations
+        eng.commit(np.ones(1, np.int32))
+    eng.close()
