@@ -1232,7 +1232,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     eb_sim_stats& q = h->stats[s];
     if (!act[s]) continue;
     int stt = status[s];
-    if (!std::isfinite(res[s]) || !std::isfinite(dn[s])) stt = EB_SIM_NAN;
+    if (stt != EB_SIM_WAIT_TIMEOUT && (!std::isfinite(res[s]) || !std::isfinite(dn[s]))) stt = EB_SIM_NAN;
     if (k[s] > P.max_iterations && stt == EB_SIM_OK) stt = EB_SIM_NOT_CONVERGED;
     if (stt == EB_SIM_WAIT_TIMEOUT) {
       // the step's solves are not trusted: report "not converged" (the caller rolls back)

@@ -42,7 +42,7 @@ void launch_band_fill(const Dev& d, const BandDev& B, const int* blk_row, cudaSt
 // of kLuThreads threads).  Per panel of kPanel columns:
 //   1. panel (rows k0 .. k0+kb+b) factorised in shared memory, column = lane;
 //   2. U12 = L11⁻¹ A12, one thread per column of U12 (independent columns);
-//   3. A22 -= L21 U12 on 4x4 register tiles, A22 read and written in place;
+//   3. A22 -= L21 U12 on 8x8 register tiles, A22 read and written in place;
 //   4. inverses of the unit-lower L11 and upper U11 stored for the solves.
 constexpr int kLuThreads = 256;
 
@@ -138,10 +138,17 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
     // columns (thread (ti, tj) owns rows ti + a R and columns tj + c R, R = ceil(q / 8)):
     // consecutive lanes read consecutive panel rows (no bank conflicts), share the U12
     // row (broadcast) and update consecutive band entries (coalesced).
+    // The tile's band entries are loaded before the product loop so their global-memory
+    // latency overlaps the FMAs.
     const int R = (q + 7) >> 3;
     for (int tile = threadIdx.x; tile < R * R; tile += kLuThreads) {
       const int ti = tile % R, tj = tile / R;
-      float acc[8][8];
+      float acc[8][8], old[8][8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+          old[a][c] = (ti + a * R < q && tj + c * R < q) ? V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) : 0.f;
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
@@ -161,7 +168,7 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
       for (int c = 0; c < 8; ++c)
 #pragma unroll
         for (int a = 0; a < 8; ++a)
-          if (ti + a * R < q && tj + c * R < q) V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) -= acc[a][c];
+          if (ti + a * R < q && tj + c * R < q) V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) = old[a][c] - acc[a][c];
     }
     // ---- write back panel and U12
     if (lane < kb)

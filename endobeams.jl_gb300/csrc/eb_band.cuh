@@ -35,7 +35,8 @@ struct BandDev {
                             // (largest first, so the last wave holds the smallest simulations)
 };
 
-constexpr int kPanel = 32;  // panel width of the blocked factorisation and solves
+constexpr int kPanel = 32;     // panel width of the blocked factorisation and solves
+constexpr int kWindow = 1024;  // shared ring of solve-vector rows (covers half bandwidths up to 960)
 
 __host__ __device__ __forceinline__ int64_t pad32(int64_t x) { return ((x + 31) / 32) * 32 + 32; }
 __host__ __device__ __forceinline__ int64_t ustride(int64_t n, int b) { return pad32(n * (int64_t)(b + 1)); }
@@ -115,6 +116,21 @@ __device__ __forceinline__ void stage_drain(const Stage* st) {
     if (st->pend[sb] >= 0) mbar_wait(&st->bar[sb], (uint32_t)st->pend[sb]);
 }
 
+// One warp: xb[0..kb) <- Binv xb (Binv a 32x32 column-major diagonal-block
+// inverse), also copied to yb.  Fully unrolled so the loads run ahead of the
+// FMA chain.
+__device__ __forceinline__ void diag_block(const float* Binv, float* xb, int kb, int lane, float* yb) {
+  float acc = 0.f;
+#pragma unroll
+  for (int t = 0; t < kPanel; ++t)
+    if (t < kb) acc = fmaf(Binv[t * kPanel + lane], xb[t], acc);
+  __syncwarp();
+  if (lane < kb) {
+    xb[lane] = acc;
+    yb[lane] = acc;
+  }
+}
+
 // z = M⁻¹ v on the CTA owning simulation s: gather into band order, forward
 // substitution with unit L, backward substitution with U, scatter back.  The
 // diagonal blocks are applied through their precomputed inverses (a 32x32
@@ -139,6 +155,19 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (n + kPanel - 1) / kPanel;
+  // Without `xs`, the sweeps keep the rows they touch in a shared ring of W >= b + 64
+  // entries (row i in slot i mod W) and exchange 32 rows with global memory per block,
+  // so the sequential chain reads and writes only shared memory.
+  __shared__ float xw[kWindow];
+  int W = kPanel * 2;
+  while (W < b + 2 * kPanel) W <<= 1;
+  const bool win = !xs && W <= kWindow;
+  const int wm = W - 1;
+  auto X = [&](int i) -> float& { return win ? xw[i & wm] : x[i]; };
+  if (win) {
+    for (int r = threadIdx.x; r < min(n, W); r += blockDim.x) xw[r & wm] = x[r];
+    __syncthreads();
+  }
   // issue the bulk copies of block jb of the L (lower) or U part into buffer `sb`
   auto issue = [&](int jb, int sb, bool lower) {
     const int k0 = jb * kPanel;
@@ -175,33 +204,51 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     const float* Lin = Li + (int64_t)k0 * kPanel;
     if (staged) {
       await(sb);
-      Lc = st->buf[sb];
-      Lin = st->inv[sb];
-    }
-    if (warp == 0) {
-      float acc = 0.f;
-      for (int t = 0; t < kb; ++t) acc += Lin[t * kPanel + lane] * x[k0 + t];
-      __syncwarp();
-      if (lane < kb) {
-        x[k0 + lane] = acc;
-        yb[lane] = acc;
+      if (!*st->fail) {  // after a wait ran out, the rest of the sweep reads global memory
+        Lc = st->buf[sb];
+        Lin = st->inv[sb];
       }
     }
+    if (warp == 0) diag_block(Lin, &X(k0), kb, lane, yb);
     __syncthreads();
+    // rows below the block, up to 4 per thread with independent accumulators; each row
+    // sums its in-band terms in increasing t (the same order staged or not)
     const int r1 = min(n, k0 + kb + b);
-    for (int i = k0 + kb + threadIdx.x; i < r1; i += blockDim.x) {
-      float acc = 0.f;
-      const int t0 = max(k0, i - b);
-      if (Lc)
-        for (int t = t0; t < k0 + kb; ++t) acc += Lc[(int64_t)(t - k0) * b + (i - t - 1)] * yb[t - k0];
-      else
-        for (int t = t0; t < k0 + kb; ++t) acc += V.at(i, t) * yb[t - k0];
-      x[i] -= acc;
+    for (int i0 = k0 + kb + (int)threadIdx.x; i0 < r1; i0 += 4 * (int)blockDim.x) {
+      int ii[4];
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) ii[q] = i0 + q * (int)blockDim.x;
+#pragma unroll 8
+      for (int t = 0; t < kPanel; ++t) {
+        if (t >= kb) break;
+        const float y = yb[t];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int d = ii[q] - (k0 + t);  // >= 1: the row is below the column
+          if (ii[q] < r1 && d <= b) {
+            const float lv = Lc ? Lc[(int64_t)t * b + (d - 1)] : V.at(ii[q], k0 + t);
+            acc[q] = fmaf(lv, y, acc[q]);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (ii[q] < r1) X(ii[q]) -= acc[q];
+    }
+    if (win && (int)threadIdx.x < kb) {  // rows k0.. leave the ring, rows k0 + W.. enter
+      const int t = threadIdx.x;
+      x[k0 + t] = xw[(k0 + t) & wm];
+      if (k0 + W + t < n) xw[(k0 + t) & wm] = x[k0 + W + t];
     }
     __syncthreads();
     if (staged && threadIdx.x == 0 && jb + 2 < nblk && !*st->fail) issue(jb + 2, sb, true);
   }
   // ---- backward: U x = y
+  if (win) {
+    for (int r = max(0, n - W) + threadIdx.x; r < n; r += blockDim.x) xw[r & wm] = x[r];
+    __syncthreads();
+  }
   if (staged && threadIdx.x == 0 && !*st->fail) {
     issue(nblk - 1, 0, false);
     if (nblk > 1) issue(nblk - 2, 1, false);
@@ -215,28 +262,41 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     const float* Uin = Ui + (int64_t)k0 * kPanel;
     if (staged) {
       await(sb);
-      Uc = st->buf[sb];
-      Uin = st->inv[sb];
-    }
-    if (warp == 0) {
-      float acc = 0.f;
-      for (int t = 0; t < kb; ++t) acc += Uin[t * kPanel + lane] * x[k0 + t];
-      __syncwarp();
-      if (lane < kb) {
-        x[k0 + lane] = acc;
-        yb[lane] = acc;
+      if (!*st->fail) {
+        Uc = st->buf[sb];
+        Uin = st->inv[sb];
       }
     }
+    if (warp == 0) diag_block(Uin, &X(k0), kb, lane, yb);
     __syncthreads();
+    // rows above the block (same scheme as the forward sweep)
     const int r0 = max(0, k0 - b);
-    for (int i = r0 + threadIdx.x; i < k0; i += blockDim.x) {
-      float acc = 0.f;
-      const int t1 = min(k0 + kb, i + b + 1);
-      if (Uc)
-        for (int t = k0; t < t1; ++t) acc += Uc[(int64_t)(t - k0) * (b + 1) + (b + i - t)] * yb[t - k0];
-      else
-        for (int t = k0; t < t1; ++t) acc += V.at(i, t) * yb[t - k0];
-      x[i] -= acc;
+    for (int i0 = r0 + (int)threadIdx.x; i0 < k0; i0 += 4 * (int)blockDim.x) {
+      int ii[4];
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) ii[q] = i0 + q * (int)blockDim.x;
+#pragma unroll 8
+      for (int t = 0; t < kPanel; ++t) {
+        if (t >= kb) break;
+        const float y = yb[t];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int d = (k0 + t) - ii[q];  // >= 1: the row is above the column
+          if (ii[q] < k0 && d <= b) {
+            const float uv = Uc ? Uc[(int64_t)t * (b + 1) + (b - d)] : V.at(ii[q], k0 + t);
+            acc[q] = fmaf(uv, y, acc[q]);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (ii[q] < k0) X(ii[q]) -= acc[q];
+    }
+    if (win && (int)threadIdx.x < kb) {  // rows k0.. leave the ring, rows k0 - W.. enter
+      const int t = threadIdx.x;
+      x[k0 + t] = xw[(k0 + t) & wm];
+      if (k0 - W + t >= 0) xw[(k0 + t) & wm] = x[k0 - W + t];
     }
     __syncthreads();
     if (staged && threadIdx.x == 0 && q + 2 < nblk && !*st->fail) issue(nblk - 1 - (q + 2), sb, false);

@@ -42,6 +42,6 @@ void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream
 cudaError_t launch_gmres(const SolverArgs& a, bool fp32, int threads, cudaStream_t s);
 size_t gmres_smem(int m);
 size_t gmres_smem_total(const SolverArgs& a);  // dynamic shared memory of one launch
-constexpr size_t kGmresSmemLimit = 220 * 1024;  // leaves room for the kernel's static shared memory
+constexpr size_t kGmresSmemLimit = 216 * 1024;  // leaves room for the kernel's static shared memory (ring, barriers)
 
 }  // namespace eb
