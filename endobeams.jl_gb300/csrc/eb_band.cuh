@@ -99,46 +99,39 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-// Shared-memory staging of a simulation's band blocks (double buffered).
+// Shared-memory staging of a simulation's band blocks: two buffers of band
+// columns (32 columns of one band part) and two of 32x32 diagonal-block
+// inverses, each pair on its own two mbarriers.
 struct Stage {
   float* buf[2];    // 32 columns of one band part: 32 (b_max + 1) floats each
-  float* inv[2];    // the matching 32x32 diagonal-block inverse
-  uint64_t* bar;    // two mbarriers
+  float* inv[2];    // 32x32 diagonal-block inverses
+  uint64_t* bar;    // four mbarriers: bar[0..1] band buffers, bar[2..3] inverse buffers
   int* fail;        // shared flag: a wait ran out (staging is then abandoned)
-  int* pend;        // shared, thread 0 only: parity of the copy in flight per buffer, -1 none
-  uint32_t extra;   // bytes expected beyond the copies on the first block (timeout-path test; normally 0)
+  int* pend;        // shared, thread 0 only: parity of the copy in flight per barrier, -1 none
+  uint32_t extra;   // bytes expected beyond the copy of the first inverse (timeout-path test; normally 0)
 };
 
 // Thread 0, at kernel end after a failed wait: waits (bounded) for copies still in flight.
 __device__ __forceinline__ void stage_drain(const Stage* st) {
   if (!st || threadIdx.x != 0) return;
-  for (int sb = 0; sb < 2; ++sb)
-    if (st->pend[sb] >= 0) mbar_wait(&st->bar[sb], (uint32_t)st->pend[sb]);
-}
-
-// One warp: xb[0..kb) <- Binv xb (Binv a 32x32 column-major diagonal-block
-// inverse), also copied to yb.  Fully unrolled so the loads run ahead of the
-// FMA chain.
-__device__ __forceinline__ void diag_block(const float* Binv, float* xb, int kb, int lane, float* yb) {
-  float acc = 0.f;
-#pragma unroll
-  for (int t = 0; t < kPanel; ++t)
-    if (t < kb) acc = fmaf(Binv[t * kPanel + lane], xb[t], acc);
-  __syncwarp();
-  if (lane < kb) {
-    xb[lane] = acc;
-    yb[lane] = acc;
-  }
+  for (int k = 0; k < 4; ++k)
+    if (st->pend[k] >= 0) mbar_wait(&st->bar[k], (uint32_t)st->pend[k]);
 }
 
 // z = M⁻¹ v on the CTA owning simulation s: gather into band order, forward
-// substitution with unit L, backward substitution with U, scatter back.  The
-// diagonal blocks are applied through their precomputed inverses (a 32x32
-// product per block), the off-diagonal band by a row-parallel update.
-// `xs` (may be null) is shared-memory room for the n permuted entries.
-// With `st` non-null, each block's 32 band columns and its inverse are
-// streamed into shared memory by bulk async copies one block ahead; `ph`
-// holds the two barriers' next phase bits and is advanced here.
+// substitution with unit L, backward substitution with U, scatter back.
+//
+// Each sweep is a look-ahead pipeline over 32-row blocks with one CTA barrier
+// per block.  At step s of the forward sweep warp 0 applies block s-1 to the
+// rows of block s ("near" rows) and solves block s with its precomputed
+// diagonal inverse, while the other warps apply block s-1 to the rows below
+// block s ("far" rows); every row receives its block contributions in
+// increasing block order, so the result does not depend on timing.  The
+// backward sweep is the mirror image.  `xs` (may be null) is shared-memory
+// room for the n permuted entries; without it the rows the sweeps touch live
+// in a shared ring.  With `st` non-null, band columns and inverses are
+// streamed into shared memory by bulk async copies one step ahead; `ph`
+// (4 entries) holds the barriers' next phase bits and is advanced here.
 template <typename TV, typename TZ>
 __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV* __restrict__ v, TZ* __restrict__ z,
                            float* xs, const Stage* st, uint32_t* ph) {
@@ -147,7 +140,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
   float* x = xs ? xs : B.work + 6 * n0;
   const float* Li = B.Linv + inv_base(n0, s);
   const float* Ui = B.Uinv + inv_base(n0, s);
-  __shared__ float yb[kPanel];
+  __shared__ float yb[2][kPanel];
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
     const int node = B.node_at[n0 + r / 6];           // global id of the node at position r/6
     x[r] = (float)v[6 * (node - n0) + r % 6];
@@ -155,9 +148,9 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (n + kPanel - 1) / kPanel;
-  // Without `xs`, the sweeps keep the rows they touch in a shared ring of W >= b + 64
-  // entries (row i in slot i mod W) and exchange 32 rows with global memory per block,
-  // so the sequential chain reads and writes only shared memory.
+  // Without `xs`, the rows the sweeps touch live in a shared ring of W >= b + 64
+  // entries (row i in slot i mod W); warp 0 exchanges each finished block with
+  // global memory (the refill value is stored into the ring one step later).
   __shared__ float xw[kWindow];
   int W = kPanel * 2;
   while (W < b + 2 * kPanel) W <<= 1;
@@ -168,139 +161,199 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     for (int r = threadIdx.x; r < min(n, W); r += blockDim.x) xw[r & wm] = x[r];
     __syncthreads();
   }
-  // issue the bulk copies of block jb of the L (lower) or U part into buffer `sb`
-  auto issue = [&](int jb, int sb, bool lower) {
+  // bulk copies: band columns of block jb (L or U part) into buffer sb, or its inverse into buffer sb
+  auto issue_cols = [&](int jb, int sb, bool lower) {
     const int k0 = jb * kPanel;
     const int kb = min(kPanel, n - k0);
     const int64_t colw = lower ? b : b + 1;
     const float* src = lower ? V.L + (int64_t)b * k0 : V.U + (int64_t)(b + 1) * k0;
     const uint32_t bytes = (uint32_t)(((int64_t)kb * colw * 4 + 15) & ~(int64_t)15);
-    const float* isrc = (lower ? Li : Ui) + (int64_t)k0 * kPanel;
     fence_async_smem();
-    mbar_expect_tx(&st->bar[sb], bytes + 4096u + (jb == 0 && lower ? st->extra : 0u));
+    mbar_expect_tx(&st->bar[sb], bytes);
     bulk_g2s(st->buf[sb], src, bytes, &st->bar[sb]);
-    bulk_g2s(st->inv[sb], isrc, 4096u, &st->bar[sb]);
     st->pend[sb] = (int)ph[sb];
   };
-  // all threads wait for buffer sb; thread 0 clears its pending mark
-  auto await = [&](int sb) {
+  auto issue_inv = [&](int jb, int sb, bool lower, uint32_t extra) {
+    const float* isrc = (lower ? Li : Ui) + (int64_t)jb * kPanel * kPanel;
+    fence_async_smem();
+    mbar_expect_tx(&st->bar[2 + sb], 4096u + extra);
+    bulk_g2s(st->inv[sb], isrc, 4096u, &st->bar[2 + sb]);
+    st->pend[2 + sb] = (int)ph[2 + sb];
+  };
+  auto await = [&](int k) {  // k: barrier index 0..3
     if (!*st->fail) {
-      if (!mbar_wait(&st->bar[sb], ph[sb]) && !mbar_wait(&st->bar[sb], ph[sb])) *st->fail = 1;
-      else if (threadIdx.x == 0) st->pend[sb] = -1;
+      if (!mbar_wait(&st->bar[k], ph[k]) && !mbar_wait(&st->bar[k], ph[k])) *st->fail = 1;
+      else if (threadIdx.x == 0) st->pend[k] = -1;
     }
-    ph[sb] ^= 1u;
+    ph[k] ^= 1u;
   };
   const bool staged = st && !*st->fail;  // uniform: read after the barrier above
-  // ---- forward: L y = x (unit diagonal)
-  if (staged && threadIdx.x == 0) {
-    issue(0, 0, true);
-    if (nblk > 1) issue(1, 1, true);
-  }
-  for (int jb = 0; jb < nblk; ++jb) {
-    const int k0 = jb * kPanel;
-    const int kb = min(kPanel, n - k0);
-    const int sb = jb & 1;
-    const float* Lc = nullptr;
-    const float* Lin = Li + (int64_t)k0 * kPanel;
-    if (staged) {
-      await(sb);
-      if (!*st->fail) {  // after a wait ran out, the rest of the sweep reads global memory
-        Lc = st->buf[sb];
-        Lin = st->inv[sb];
+
+  for (int sweep = 0; sweep < 2; ++sweep) {
+    const bool fwd = sweep == 0;
+    const float* Ig = fwd ? Li : Ui;
+    if (!fwd && win) {
+      for (int r = max(0, n - W) + threadIdx.x; r < n; r += blockDim.x) xw[r & wm] = x[r];
+      __syncthreads();
+    }
+    // block visited at step q (forward: q, backward: nblk - 1 - q)
+    auto blk = [&](int q) { return fwd ? q : nblk - 1 - q; };
+    if (staged && threadIdx.x == 0 && !*st->fail) {
+      issue_inv(blk(0), 0, fwd, fwd ? st->extra : 0u);
+      if (nblk > 1) {
+        issue_inv(blk(1), 1, fwd, 0u);
+        issue_cols(blk(0), 0, fwd);
       }
     }
-    if (warp == 0) diag_block(Lin, &X(k0), kb, lane, yb);
-    __syncthreads();
-    // rows below the block, up to 4 per thread with independent accumulators; each row
-    // sums its in-band terms in increasing t (the same order staged or not)
-    const int r1 = min(n, k0 + kb + b);
-    for (int i0 = k0 + kb + (int)threadIdx.x; i0 < r1; i0 += 4 * (int)blockDim.x) {
-      int ii[4];
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    float pv = 0.f;       // warp 0: ring refill value loaded at the previous step
+    int pslot = -1;
+    for (int q = 0; q < nblk; ++q) {
+      const int jb = blk(q);
+      const int k0 = jb * kPanel;
+      const int kb = min(kPanel, n - k0);
+      // the block applied at this step (previous in sweep order) and its columns
+      const int pj = q > 0 ? blk(q - 1) : -1;
+      const int pk0 = pj * kPanel;
+      const int pkb = q > 0 ? min(kPanel, n - pk0) : 0;
+      const float* Pc = nullptr;                                  // staged columns of block pj
+      const float* Inv = Ig + (int64_t)k0 * kPanel;               // inverse of block jb
+      if (staged) {
+        if (q > 0) await((q - 1) & 1);
+        if (warp == 0) await(2 + (q & 1));
+        if (!*st->fail) {
+          if (q > 0) Pc = st->buf[(q - 1) & 1];
+          Inv = st->inv[q & 1];
+        }
+      }
+      const float* yp = yb[(q + 1) & 1];  // y of block pj (written at step q - 1)
+      if (warp == 0) {
+        if (pslot >= 0) xw[pslot] = pv;  // refill from the previous step
+        pslot = -1;
+        // near rows: the rows of block jb receive block pj
+        if (q > 0 && lane < kb) {
+          const int i = k0 + lane;
+          float a0 = 0.f, a1 = 0.f;
+          if (fwd) {  // L(i, pk0 + t), d = i - pk0 - t in [1, b]
+            const int tlo = max(0, i - pk0 - b);
+            int t = tlo;
+            if (Pc) {
+              const float* col = Pc + (i - pk0 - 1);
+              for (; t + 1 < pkb; t += 2) {
+                a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+                a1 = fmaf(col[(t + 1) * (b - 1)], yp[t + 1], a1);
+              }
+              if (t < pkb) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+            } else {
+              for (; t + 1 < pkb; t += 2) {
+                a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+                a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+              }
+              if (t < pkb) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+            }
+          } else {  // U(i, pk0 + t), d = pk0 + t - i in [1, b]
+            const int thi = min(pkb, i + b - pk0 + 1);
+            int t = 0;
+            if (Pc) {
+              const float* col = Pc + (b - pk0 + i);
+              for (; t + 1 < thi; t += 2) {
+                a0 = fmaf(col[t * b], yp[t], a0);
+                a1 = fmaf(col[(t + 1) * b], yp[t + 1], a1);
+              }
+              if (t < thi) a0 = fmaf(col[t * b], yp[t], a0);
+            } else {
+              for (; t + 1 < thi; t += 2) {
+                a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+                a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+              }
+              if (t < thi) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+            }
+          }
+          X(i) -= a0 + a1;
+        }
+        __syncwarp();
+        // diagonal block: y = Inv x over the block's rows (two accumulators)
+        float d0 = 0.f, d1 = 0.f;
+        float* xb = &X(k0);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) ii[q] = i0 + q * (int)blockDim.x;
-#pragma unroll 8
-      for (int t = 0; t < kPanel; ++t) {
-        if (t >= kb) break;
-        const float y = yb[t];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int d = ii[q] - (k0 + t);  // >= 1: the row is below the column
-          if (ii[q] < r1 && d <= b) {
-            const float lv = Lc ? Lc[(int64_t)t * b + (d - 1)] : V.at(ii[q], k0 + t);
-            acc[q] = fmaf(lv, y, acc[q]);
+        for (int t = 0; t < kPanel; t += 2) {
+          if (t < kb) d0 = fmaf(Inv[t * kPanel + lane], xb[t], d0);
+          if (t + 1 < kb) d1 = fmaf(Inv[(t + 1) * kPanel + lane], xb[t + 1], d1);
+        }
+        __syncwarp();
+        if (lane < kb) {
+          const float y = d0 + d1;
+          xb[lane] = y;
+          yb[q & 1][lane] = y;
+          if (win) {  // the block is final: write it back, load the row that takes its slot
+            x[k0 + lane] = y;
+            const int nr = fwd ? k0 + W + lane : k0 - W + lane;
+            if (nr >= 0 && nr < n) {
+              pv = x[nr];
+              pslot = (k0 + lane) & wm;
+            }
+          }
+        }
+      } else if (q > 0) {
+        // far rows receive block pj (threads of warps 1.. only)
+        const int tid = threadIdx.x - 32, nth = blockDim.x - 32;
+        if (fwd) {
+          const int r1 = min(n, pk0 + pkb + b);
+          for (int i = pk0 + 2 * kPanel + tid; i < r1; i += nth) {
+            const int tlo = max(0, i - pk0 - b);
+            float a0 = 0.f, a1 = 0.f;
+            int t = tlo;
+            if (Pc) {
+              const float* col = Pc + (i - pk0 - 1);
+              for (; t + 1 < pkb; t += 2) {
+                a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+                a1 = fmaf(col[(t + 1) * (b - 1)], yp[t + 1], a1);
+              }
+              if (t < pkb) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+            } else {
+              for (; t + 1 < pkb; t += 2) {
+                a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+                a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+              }
+              if (t < pkb) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+            }
+            X(i) -= a0 + a1;
+          }
+        } else {
+          const int r0 = max(0, pk0 - b);
+          for (int i = r0 + tid; i < pk0 - kPanel; i += nth) {
+            const int thi = min(pkb, i + b - pk0 + 1);
+            float a0 = 0.f, a1 = 0.f;
+            int t = 0;
+            if (Pc) {
+              const float* col = Pc + (b - pk0 + i);
+              for (; t + 1 < thi; t += 2) {
+                a0 = fmaf(col[t * b], yp[t], a0);
+                a1 = fmaf(col[(t + 1) * b], yp[t + 1], a1);
+              }
+              if (t < thi) a0 = fmaf(col[t * b], yp[t], a0);
+            } else {
+              for (; t + 1 < thi; t += 2) {
+                a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+                a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+              }
+              if (t < thi) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+            }
+            X(i) -= a0 + a1;
           }
         }
       }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (ii[q] < r1) X(ii[q]) -= acc[q];
-    }
-    if (win && (int)threadIdx.x < kb) {  // rows k0.. leave the ring, rows k0 + W.. enter
-      const int t = threadIdx.x;
-      x[k0 + t] = xw[(k0 + t) & wm];
-      if (k0 + W + t < n) xw[(k0 + t) & wm] = x[k0 + W + t];
-    }
-    __syncthreads();
-    if (staged && threadIdx.x == 0 && jb + 2 < nblk && !*st->fail) issue(jb + 2, sb, true);
-  }
-  // ---- backward: U x = y
-  if (win) {
-    for (int r = max(0, n - W) + threadIdx.x; r < n; r += blockDim.x) xw[r & wm] = x[r];
-    __syncthreads();
-  }
-  if (staged && threadIdx.x == 0 && !*st->fail) {
-    issue(nblk - 1, 0, false);
-    if (nblk > 1) issue(nblk - 2, 1, false);
-  }
-  for (int q = 0; q < nblk; ++q) {
-    const int jb = nblk - 1 - q;
-    const int k0 = jb * kPanel;
-    const int kb = min(kPanel, n - k0);
-    const int sb = q & 1;
-    const float* Uc = nullptr;
-    const float* Uin = Ui + (int64_t)k0 * kPanel;
-    if (staged) {
-      await(sb);
-      if (!*st->fail) {
-        Uc = st->buf[sb];
-        Uin = st->inv[sb];
+      __syncthreads();
+      // buffers freed at this step: band columns of block pj, inverse of block jb
+      if (staged && threadIdx.x == 0 && !*st->fail) {
+        if (q + 1 <= nblk - 2) issue_cols(blk(q + 1), (q + 1) & 1, fwd);
+        if (q + 2 <= nblk - 1) issue_inv(blk(q + 2), q & 1, fwd, 0u);
       }
     }
-    if (warp == 0) diag_block(Uin, &X(k0), kb, lane, yb);
+    if (warp == 0 && pslot >= 0) xw[pslot] = pv;
+    if (!win) continue;
     __syncthreads();
-    // rows above the block (same scheme as the forward sweep)
-    const int r0 = max(0, k0 - b);
-    for (int i0 = r0 + (int)threadIdx.x; i0 < k0; i0 += 4 * (int)blockDim.x) {
-      int ii[4];
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-      for (int q = 0; q < 4; ++q) ii[q] = i0 + q * (int)blockDim.x;
-#pragma unroll 8
-      for (int t = 0; t < kPanel; ++t) {
-        if (t >= kb) break;
-        const float y = yb[t];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int d = (k0 + t) - ii[q];  // >= 1: the row is above the column
-          if (ii[q] < k0 && d <= b) {
-            const float uv = Uc ? Uc[(int64_t)t * (b + 1) + (b - d)] : V.at(ii[q], k0 + t);
-            acc[q] = fmaf(uv, y, acc[q]);
-          }
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (ii[q] < k0) X(ii[q]) -= acc[q];
-    }
-    if (win && (int)threadIdx.x < kb) {  // rows k0.. leave the ring, rows k0 - W.. enter
-      const int t = threadIdx.x;
-      x[k0 + t] = xw[(k0 + t) & wm];
-      if (k0 - W + t >= 0) xw[(k0 + t) & wm] = x[k0 - W + t];
-    }
-    __syncthreads();
-    if (staged && threadIdx.x == 0 && q + 2 < nblk && !*st->fail) issue(nblk - 1 - (q + 2), sb, false);
   }
+  __syncthreads();
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
     const int node = B.node_at[n0 + r / 6];
     z[6 * (node - n0) + r % 6] = (TZ)x[r];

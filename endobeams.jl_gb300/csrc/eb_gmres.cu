@@ -112,12 +112,12 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   const bool use_band = a.band.bw != nullptr && a.band.bw[s] > 0;
   float* xs = a.x_in_smem ? reinterpret_cast<float*>(red + 8 * 32) : nullptr;  // permuted solve vector
   // shared-memory staging of band blocks for the triangular solves (bulk async copies)
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) uint64_t bars[4];
   __shared__ int stage_fail;
-  __shared__ int stage_pend[2];
+  __shared__ int stage_pend[4];
   Stage stage;
   const Stage* stp = nullptr;
-  uint32_t ph[2] = {0u, 0u};
+  uint32_t ph[4] = {0u, 0u, 0u, 0u};
   if (use_band && a.stage_floats > 0) {
     char* base = reinterpret_cast<char*>(xs ? xs + a.max_n : reinterpret_cast<float*>(red + 8 * 32));
     base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 127) & ~uintptr_t(127));
@@ -131,10 +131,11 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
     stage.pend = stage_pend;
     stage.extra = (uint32_t)a.stage_test_extra;
     if (threadIdx.x == 0) {
-      mbar_init(&bars[0], 1);
-      mbar_init(&bars[1], 1);
+      for (int k = 0; k < 4; ++k) {
+        mbar_init(&bars[k], 1);
+        stage_pend[k] = -1;
+      }
       stage_fail = 0;
-      stage_pend[0] = stage_pend[1] = -1;
       fence_async_smem();
     }
     __syncthreads();
