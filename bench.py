@@ -59,7 +59,7 @@ STENT_TOL_DISP = 1e-8
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="stents1024")
@@ -86,9 +86,9 @@ def stent_params(p, precision="mixed", warm="off"):
     p.tolerance_residual = STENT_TOL_RES
     p.tolerance_displacement = STENT_TOL_DISP
     p.krylov_restart = 32
-    # the stents' band LU costs ~0.1-1 s per factorisation on one SM: reuse it while GMRES needs <= 48
-    # iterations (measured on 64 stents: 12.8 steps/s at 48 against 10.9 at 16)
-    p.refactor_its = 48
+    # the stents' band LU costs ~0.1-1 s per factorisation on one SM: reuse it while GMRES needs <= 200
+    # iterations (64 stents: 20.1 HHT steps/s never refactorising, 17.9 at 48, 14.5 at 16)
+    p.refactor_its = 200
     p.precision = precision
     p.warm_start = warm
     return p
@@ -112,8 +112,12 @@ class Workload:
             self.warm = "off"
             self.sdf = None
         else:
+            import re
+            m = re.fullmatch(r"stent(\d+)x(\d+)", name)
             if name == "stent":
                 self.variants = [None]
+            elif m:  # one stent with the given wires x elements per wire (profiling size)
+                self.variants = [("custom", int(m.group(1)), int(m.group(2)))]
             elif name.startswith("stents"):
                 n = count or int(name[len("stents"):] or 1024)
                 self.variants = scenes.stent_variants(1024, seed=2)[:n]
@@ -121,7 +125,7 @@ class Workload:
                 raise SystemExit(f"unknown workload {name}")
             self.count = len(self.variants)
             self.precision = precision or "mixed"
-            self.warm = warm or ("learned" if (name != "stent" and os.path.exists(MODEL)) else "off")
+            self.warm = warm or ("learned" if (name.startswith("stents") and os.path.exists(MODEL)) else "off")
 
     def stats(self, i):
         """(nodes, elements, RCM half bandwidth in nodes, SDF points, Krylov restart) of simulation i (cached)."""
@@ -147,7 +151,12 @@ class Workload:
             p.precision = self.precision
             return c, p, it
         v = self.variants[i]
-        c, p, it = s.braided_stent() if v is None else s.stent_variant(v)
+        if v is None:
+            c, p, it = s.braided_stent()
+        elif isinstance(v, tuple):
+            c, p, it = s.braided_stent(wires=v[1], elems_per_wire=v[2], grid=None)
+        else:
+            c, p, it = s.stent_variant(v)
         return c, stent_params(p, self.precision, self.warm), it
 
     def describe(self, nodes, elements, groups):

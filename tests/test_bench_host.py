@@ -1,0 +1,32 @@
+"""Host-side pieces of bench.py: workload naming, the device-memory estimator and
+the resident-group planner (no GPU needed)."""
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def test_workload_names_and_population():
+    import bench
+    wl = bench.Workload("stents1024")
+    assert wl.count == 1024 and wl.kind == "stents" and wl.precision == "mixed"
+    c, p, it = wl.build(0)
+    assert p.tolerance_residual == bench.STENT_TOL_RES and p.krylov_restart == 32
+    one = bench.Workload("stent24x60")
+    c, p, it = one.build(0)
+    assert len(c.beams) == 24 * 60 and one.warm == "off"
+    nets = bench.Workload("nets16")
+    assert nets.count == 16 and nets.warm == "off"
+
+
+def test_memory_estimate_and_groups():
+    import bench
+    wl = bench.Workload("stents1024", count=12)
+    sizes = [bench.est_bytes(wl.stats(i)) for i in range(12)]
+    # a stent holds 0.1-0.7 GB (the 64-stent batch measured 17.3 GB; estimator 17.7 GB)
+    assert all(0.05e9 < s < 1.0e9 for s in sizes), sizes
+    groups = bench.plan_groups(wl, int(1.01 * max(sizes) * 3))
+    assert sum(len(g) for g in groups) == 12 and [i for g in groups for i in g] == list(range(12))
+    assert all(sum(sizes[i] for i in g) <= 1.01 * max(sizes) * 3 or len(g) == 1 for g in groups)
+    assert len(bench.plan_groups(wl, 10 ** 15)) == 1
