@@ -285,6 +285,9 @@ struct WsHost {
   double* d_rn = nullptr;      // 2 n_sims residual norms
   std::vector<double> rn;
   std::vector<int> used;
+  std::vector<int> tried;      // this step: the simulation started from the network
+  std::vector<int> streak;     // consecutive rejected learned starts
+  std::vector<int> skip;       // steps left before the next learned attempt (back-off)
   ~WsHost() {
     cudaFree(F); cudaFree(X); cudaFree(Y); cudaFree(norm); cudaFree(P); cudaFree(W); cudaFree(sF); cudaFree(sT);
   }
@@ -908,7 +911,10 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     sa.stage_floats = 0;
     sa.stage_test_extra = p->stage_band == 2 ? 16 : 0;
     if (h->any_band && p->stage_band) {
+      // two band-column buffers (copies one step ahead); stage_band 3 keeps one buffer, which
+      // halves the staging memory (measured slower on 64 stents: 13.3 against 16.2 HHT steps/s)
       sa.stage_floats = kPanel * (h->max_b + 1);
+      sa.stage_nbuf = p->stage_band == 3 ? 1 : 2;
       if (gmres_smem_total(sa) > kGmresSmemLimit) sa.stage_floats = 0;
     }
   }
@@ -929,6 +935,9 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     h->ws.dev.surf_on = h->ws.d_surf_on;
     h->ws.rn.assign(2 * (size_t)n_sims, 0.0);
     h->ws.used.assign(n_sims, 0);
+    h->ws.tried.assign(n_sims, 0);
+    h->ws.streak.assign(n_sims, 0);
+    h->ws.skip.assign(n_sims, 0);
   }
 
   // ---- initialize_state_simulation! (inizialization.jl:37-44): beams only, matricesⁿ ← matricesⁿ⁺¹
@@ -1056,11 +1065,17 @@ static int learned_start_check(eb_handle* h, const std::vector<int>& running, do
   std::vector<int> fb(S, 0);
   bool any = false;
   for (int s = 0; s < S; ++s) {
-    if (!running[s]) continue;
+    if (!running[s] || !ws.tried[s]) continue;
     const double r0 = ws.rn[s], r1 = ws.rn[S + s];
     fb[s] = !(std::isfinite(r1) && r1 <= r0);
     ws.used[s] = !fb[s];
     any |= fb[s] != 0;
+    if (fb[s]) {
+      ws.streak[s] = std::min(ws.streak[s] + 1, 6);
+      ws.skip[s] = 1 << (ws.streak[s] - 1);
+    } else {
+      ws.streak[s] = 0;
+    }
   }
   if (!any) return EB_OK;
   PhaseTimer& T = h->timer;
@@ -1135,11 +1150,31 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
   T.launches[EB_PHASE_PREDICTOR] += 4;
   int rc = 0;
   if (learned) {
-    // the predictor's right-hand side norm is the fallback threshold; the network replaces its solve
-    launch_ws_rnorm(d, ws.d_rn, st);
-    CK(mlp_forward(MlpDev{ws.P, ws.W}, ws.X, d.n_nodes, ws.Y, st));
-    launch_ws_apply(d, ws.dev, st);
-    T.launches[EB_PHASE_PREDICTOR] += 3;
+    // Simulations whose learned starts were rejected recently back off (1, 2, 4 .. 64 steps)
+    // and take the HHT predictor; the others start from the network, with the predictor's
+    // right-hand side norm as the fallback threshold.
+    std::vector<int> plain(S, 0);
+    bool any_plain = false, any_try = false;
+    for (int s = 0; s < S; ++s) {
+      ws.tried[s] = act[s] && ws.skip[s] == 0;
+      plain[s] = act[s] && !ws.tried[s];
+      if (plain[s]) ws.skip[s] -= 1;
+      any_plain |= plain[s] != 0;
+      any_try |= ws.tried[s] != 0;
+    }
+    if (any_plain) {
+      CK(cudaMemcpyAsync(h->d_active, plain.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+      rc = solve(h, plain.data());
+      if (rc) return rc;
+    }
+    if (any_try) {
+      CK(cudaMemcpyAsync(h->d_active, ws.tried.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+      launch_ws_rnorm(d, ws.d_rn, st);
+      CK(mlp_forward(MlpDev{ws.P, ws.W}, ws.X, d.n_nodes, ws.Y, st));
+      launch_ws_apply(d, ws.dev, st);
+      T.launches[EB_PHASE_PREDICTOR] += 3;
+    }
+    CK(cudaMemcpyAsync(h->d_active, act.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
   } else {
     rc = solve(h, act.data());
     if (rc) return rc;
@@ -1248,8 +1283,8 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     q.last_dD_norm = dn[s];
     q.max_linear_rel_residual = rel[s];
     q.warm_start_used = learned ? ws.used[s] : 0;
-    q.predictor_rhs_norm = learned ? std::sqrt(ws.rn[s]) : 0.0;
-    q.start_res_norm = learned ? std::sqrt(ws.rn[S + s]) : 0.0;
+    q.predictor_rhs_norm = learned && ws.tried[s] ? std::sqrt(ws.rn[s]) : 0.0;
+    q.start_res_norm = learned && ws.tried[s] ? std::sqrt(ws.rn[S + s]) : 0.0;
     k_out[s] = k[s];
     if (status_out) status_out[s] = stt;
   }

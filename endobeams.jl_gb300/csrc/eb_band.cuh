@@ -22,7 +22,7 @@
 namespace eb {
 
 struct BandDev {
-  float* A;                 // concatenated band storage
+  float* A;                 // concatenated band storage (FP32: filled and factorised in place)
   const int64_t* off;       // per sim: offset of its U part in A (L part follows)
   const int* bw;            // per sim: half bandwidth b in DOFs (0: no band, block-Jacobi)
   const int* pos;           // per global node: position in its simulation's band order
@@ -109,6 +109,7 @@ struct Stage {
   int* fail;        // shared flag: a wait ran out (staging is then abandoned)
   int* pend;        // shared, thread 0 only: parity of the copy in flight per barrier, -1 none
   uint32_t extra;   // bytes expected beyond the copy of the first inverse (timeout-path test; normally 0)
+  int nbuf;         // band-column buffers: 2 = copy one step ahead, 1 = copy after the step that frees it
 };
 
 // Thread 0, at kernel end after a failed wait: waits (bounded) for copies still in flight.
@@ -202,7 +203,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       issue_inv(blk(0), 0, fwd, fwd ? st->extra : 0u);
       if (nblk > 1) {
         issue_inv(blk(1), 1, fwd, 0u);
-        issue_cols(blk(0), 0, fwd);
+        if (st->nbuf == 2) issue_cols(blk(0), 0, fwd);
       }
     }
     float pv = 0.f;       // warp 0: ring refill value loaded at the previous step
@@ -218,10 +219,10 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       const float* Pc = nullptr;                                  // staged columns of block pj
       const float* Inv = Ig + (int64_t)k0 * kPanel;               // inverse of block jb
       if (staged) {
-        if (q > 0) await((q - 1) & 1);
+        if (q > 0) await((q - 1) % st->nbuf);
         if (warp == 0) await(2 + (q & 1));
         if (!*st->fail) {
-          if (q > 0) Pc = st->buf[(q - 1) & 1];
+          if (q > 0) Pc = st->buf[(q - 1) % st->nbuf];
           Inv = st->inv[q & 1];
         }
       }
@@ -345,7 +346,8 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       __syncthreads();
       // buffers freed at this step: band columns of block pj, inverse of block jb
       if (staged && threadIdx.x == 0 && !*st->fail) {
-        if (q + 1 <= nblk - 2) issue_cols(blk(q + 1), (q + 1) & 1, fwd);
+        const int J = q + st->nbuf - 1;  // band columns needed at step J + 1
+        if (J <= nblk - 2) issue_cols(blk(J), J % st->nbuf, fwd);
         if (q + 2 <= nblk - 1) issue_inv(blk(q + 2), q & 1, fwd, 0u);
       }
     }

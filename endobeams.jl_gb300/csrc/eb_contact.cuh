@@ -186,15 +186,35 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
   const double kn = cp.kn, mu = cp.mu, eps_t = cp.eps_t;
   double eta_n = cp.eta_n;  // overwritten by each in-contact Gauss point (reference scoping)
 
+  // Which Gauss points are in contact (:72, :95).  Most elements have none: they return
+  // here, before the 12x12 accumulators are touched.
+  bool inc[3];
+  bool touched = false;
+#pragma unroll
+  for (int ig = 0; ig < 3; ++ig) {
+    const double zg = gs.z[ig];
+    double xi = l0 * (zg + 1) / 2;
+    double s = xi / l0;
+    double N1 = 1 - s, N2 = 1 - N1;
+    double N3 = xi * ((1 - s) * (1 - s));
+    double N4 = -(1 - s) * ((xi * xi) / l0);
+    V3 ut = v3(0.0, N3 * Th1.z + N4 * Th2.z, -N3 * Th1.y - N4 * Th2.y);
+    V3 xG = N1 * x1 + N2 * x2 + Re * ut;
+    inc[ig] = incontact(srf, xG, rb);
+    touched |= inc[ig];
+  }
+  *any_contact = touched;
+  if (!touched) return;
+
   double energy = 0.0;
   V3 Tc[4] = {zv3(), zv3(), zv3(), zv3()};
   M3 Kc[16], Cc[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) { Kc[k] = zm3(); Cc[k] = zm3(); }
-  bool touched = false;
 
 #pragma unroll 1
   for (int ig = 0; ig < 3; ++ig) {
+    if (!inc[ig]) continue;
     const double zg = gs.z[ig], wg = gs.w[ig];
     double xi = l0 * (zg + 1) / 2;
     double s = xi / l0;
@@ -204,8 +224,6 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
     double N7 = N3 + N4;
     V3 ut = v3(0.0, N3 * Th1.z + N4 * Th2.z, -N3 * Th1.y - N4 * Th2.y);
     V3 xG = N1 * x1 + N2 * x2 + Re * ut;
-    if (!incontact(srf, xG, rb)) continue;
-    touched = true;
 
     double N7l = N7 * il, N7l2 = N7l * il;
     M3 Sut = skew(ut);
@@ -308,9 +326,6 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
       }
     }
   }
-  *any_contact = touched;
-  if (!touched) return;
-
   const double l02 = l0 / 2;
   out.E[0] = l02 * energy;
 #pragma unroll

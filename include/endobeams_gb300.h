@@ -80,14 +80,18 @@ typedef struct {
   int32_t stage_band;                     /* 1: the triangular solves stream band blocks into shared memory
                                              with bulk asynchronous copies (same arithmetic, same results);
                                              2: as 1, but the first block's wait expects 16 bytes that no copy
-                                             delivers, so it runs out (tests EB_SIM_WAIT_TIMEOUT) */
+                                             delivers, so it runs out (tests EB_SIM_WAIT_TIMEOUT);
+                                             3: one band-column buffer instead of two (half the staging
+                                             memory; the copy then starts after the step that frees it) */
   int32_t warm_start;                     /* EB_WS_OFF | EB_WS_LEARNED (needs eb_ws_set_model) */
 } eb_params;
 
 /* Newton start of each step */
 #define EB_WS_OFF 0      /* HHT predictor (predictor.jl:1-27) */
 #define EB_WS_LEARNED 1  /* per-node MLP increment; per simulation, the predictor again when the learned
-                            start's residual exceeds the predictor's right-hand side */
+                            start's residual exceeds the predictor's right-hand side; after k rejections
+                            in a row a simulation uses the predictor for 2^(k-1) steps (at most 32)
+                            before trying the network again */
 
 /* GMRES preconditioner */
 #define EB_PRECOND_BAND 0          /* FP32 band LU in reverse Cuthill-McKee order (block-Jacobi where it does not fit) */

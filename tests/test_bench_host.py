@@ -24,8 +24,8 @@ def test_memory_estimate_and_groups():
     import bench
     wl = bench.Workload("stents1024", count=12)
     sizes = [bench.est_bytes(wl.stats(i)) for i in range(12)]
-    # a stent holds 0.1-0.7 GB (the 64-stent batch measured 17.3 GB; estimator 17.7 GB)
-    assert all(0.05e9 < s < 1.0e9 for s in sizes), sizes
+    # a stent holds 0.1-0.8 GB (the 64-stent batch measured 17.3 GB; estimator 17.7 GB)
+    assert all(0.05e9 < s < 1.5e9 for s in sizes), sizes
     groups = bench.plan_groups(wl, int(1.01 * max(sizes) * 3))
     assert sum(len(g) for g in groups) == 12 and [i for g in groups for i in g] == list(range(12))
     assert all(sum(sizes[i] for i in g) <= 1.01 * max(sizes) * 3 or len(g) == 1 for g in groups)
