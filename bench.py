@@ -334,17 +334,19 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
         n_loaded = sum(len(c.loads.concentrated_force.loaded_dofs) for c in confs if c.loads is not None)
         drv.reset()
         barrier(world)
+        eng.timer_start()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             drv.step(e2e=True, ubuf=ubuf)
         wall = allreduce_max(time.perf_counter() - t0, world)
+        dev_ms = eng.timer_stop()
         S = drv.S
         bi = drv.batch_iters / max(args.steps, 1)
         # loads, per-sim step constants (cK, cC, cM, dt), active masks (step + each iteration), commit mask
         h2d = 8 * n_loaded + 32 * S + 4 * S + 4 * S * bi + 4 * S
         # displacements, per-iteration Newton norms, per-step solver statistics
         d2h = 24 * total_nodes + 40 * S * bi + 20 * S
-        out["e2e"] = {"sim_steps": drv.ok_steps, "wall_s": wall, "h2d": h2d, "d2h": d2h}
+        out["e2e"] = {"sim_steps": drv.ok_steps, "wall_s": wall, "h2d": h2d, "d2h": d2h, "device_ms": dev_ms}
     eng.close()
     return out
 
@@ -390,7 +392,7 @@ def gpu_arm(args, rank, world):
                 tot["phase_ms"][k] += r["phase_ms"][k]
                 tot["launches"][k] += r["launches"][k]
             if tot["e2e"] and r["e2e"]:
-                for k in ("sim_steps", "wall_s", "h2d", "d2h"):
+                for k in ("sim_steps", "wall_s", "h2d", "d2h", "device_ms"):
                     tot["e2e"][k] += r["e2e"][k]
     clk = clocks.stop()
     value = world * tot["sim_steps"] / (tot["ms"] / 1e3)
@@ -399,7 +401,8 @@ def gpu_arm(args, rank, world):
     if tot["e2e"]:
         e = tot["e2e"]
         e2e = {"value": world * e["sim_steps"] / e["wall_s"], "unit": "HHT steps/s",
-               "h2d_bytes_per_step": int(e["h2d"] / max(steps, 1)), "d2h_bytes_per_step": int(e["d2h"] / max(steps, 1))}
+               "h2d_bytes_per_step": int(e["h2d"] / max(steps, 1)), "d2h_bytes_per_step": int(e["d2h"] / max(steps, 1)),
+               "device_value": world * e["sim_steps"] / (e["device_ms"] / 1e3)}
     phase_ms, launches = tot["phase_ms"], tot["launches"]
     dom = max(phase_ms, key=lambda k: phase_ms[k])
     # ---- rooflines: the element kernel (FP64 pipe) and the Krylov kernel (HBM)

@@ -312,6 +312,7 @@ struct eb_handle {
   int64_t* d_load_dof = nullptr;
   int64_t* d_fix_dof = nullptr;
   double* d_vals = nullptr;                // scratch for set_loads / set_imposed
+  double* d_u3 = nullptr;                  // n_nodes x 3 scratch for eb_get_displacements (first use)
   // per-sim device arrays
   int* d_mask = nullptr;
   int* d_active = nullptr;
@@ -345,6 +346,12 @@ namespace {
 __global__ void k_scatter(const int64_t* idx, const double* vals, int64_t n, double* dst) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) dst[idx[t]] = vals[t];
+}
+
+// u (structure of arrays, component k at [k n + i]) -> n x 3 row-major.
+__global__ void k_interleave3(const double* __restrict__ u, int64_t n, double* __restrict__ out) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 3 * n) out[t] = u[(t % 3) * n + t / 3];
 }
 
 int upload_mask(eb_handle* h, int* dst, const int32_t* mask) {
@@ -911,10 +918,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     sa.stage_floats = 0;
     sa.stage_test_extra = p->stage_band == 2 ? 16 : 0;
     if (h->any_band && p->stage_band) {
-      // two band-column buffers (copies one step ahead); stage_band 3 keeps one buffer, which
-      // halves the staging memory (measured slower on 64 stents: 13.3 against 16.2 HHT steps/s)
       sa.stage_floats = kPanel * (h->max_b + 1);
-      sa.stage_nbuf = p->stage_band == 3 ? 1 : 2;
       if (gmres_smem_total(sa) > kGmresSmemLimit) sa.stage_floats = 0;
     }
   }
@@ -1041,12 +1045,11 @@ int eb_set_loads_all(eb_handle* h, const double* values) {
 int eb_get_displacements(eb_handle* h, double* u) {
   if (!h || !u) return fail(EB_ERR_ARG, "bad arguments");
   const int64_t NN = h->d.n_nodes;
-  std::vector<double> tmp((size_t)NN);
-  for (int k = 0; k < 3; ++k) {
-    CK(cudaMemcpyAsync(tmp.data(), h->d.u + k * NN, sizeof(double) * NN, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    for (int64_t i = 0; i < NN; ++i) u[3 * i + k] = tmp[i];
-  }
+  if (!h->d_u3) CK(h->arena.alloc(&h->d_u3, 3 * (size_t)NN));
+  if (NN) k_interleave3<<<nblocks(3 * NN, 256), 256, 0, h->stream>>>(h->d.u, NN, h->d_u3);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(u, h->d_u3, sizeof(double) * 3 * NN, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return EB_OK;
 }
 

@@ -109,7 +109,6 @@ struct Stage {
   int* fail;        // shared flag: a wait ran out (staging is then abandoned)
   int* pend;        // shared, thread 0 only: parity of the copy in flight per barrier, -1 none
   uint32_t extra;   // bytes expected beyond the copy of the first inverse (timeout-path test; normally 0)
-  int nbuf;         // band-column buffers: 2 = copy one step ahead, 1 = copy after the step that frees it
 };
 
 // Thread 0, at kernel end after a failed wait: waits (bounded) for copies still in flight.
@@ -141,7 +140,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
   float* x = xs ? xs : B.work + 6 * n0;
   const float* Li = B.Linv + inv_base(n0, s);
   const float* Ui = B.Uinv + inv_base(n0, s);
-  __shared__ float yb[2][kPanel];
+  __shared__ float yb[2][kPanel];  // y of the last two blocks
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
     const int node = B.node_at[n0 + r / 6];           // global id of the node at position r/6
     x[r] = (float)v[6 * (node - n0) + r % 6];
@@ -203,7 +202,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       issue_inv(blk(0), 0, fwd, fwd ? st->extra : 0u);
       if (nblk > 1) {
         issue_inv(blk(1), 1, fwd, 0u);
-        if (st->nbuf == 2) issue_cols(blk(0), 0, fwd);
+        issue_cols(blk(0), 0, fwd);
       }
     }
     float pv = 0.f;       // warp 0: ring refill value loaded at the previous step
@@ -219,10 +218,10 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       const float* Pc = nullptr;                                  // staged columns of block pj
       const float* Inv = Ig + (int64_t)k0 * kPanel;               // inverse of block jb
       if (staged) {
-        if (q > 0) await((q - 1) % st->nbuf);
+        if (q > 0) await((q - 1) & 1);
         if (warp == 0) await(2 + (q & 1));
         if (!*st->fail) {
-          if (q > 0) Pc = st->buf[(q - 1) % st->nbuf];
+          if (q > 0) Pc = st->buf[(q - 1) & 1];
           Inv = st->inv[q & 1];
         }
       }
@@ -346,8 +345,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       __syncthreads();
       // buffers freed at this step: band columns of block pj, inverse of block jb
       if (staged && threadIdx.x == 0 && !*st->fail) {
-        const int J = q + st->nbuf - 1;  // band columns needed at step J + 1
-        if (J <= nblk - 2) issue_cols(blk(J), J % st->nbuf, fwd);
+        if (q + 1 <= nblk - 2) issue_cols(blk(q + 1), (q + 1) & 1, fwd);
         if (q + 2 <= nblk - 1) issue_inv(blk(q + 2), q & 1, fwd, 0u);
       }
     }

@@ -121,17 +121,16 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   if (use_band && a.stage_floats > 0) {
     char* base = reinterpret_cast<char*>(xs ? xs + a.max_n : reinterpret_cast<float*>(red + 8 * 32));
     base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 127) & ~uintptr_t(127));
+    // two band-column buffers of stage_floats = 32 (b_max + 1) floats, then the inverses
     float* f = reinterpret_cast<float*>(base);
     stage.buf[0] = f;
-    stage.buf[1] = f + (a.stage_nbuf - 1) * (int64_t)a.stage_floats;
-    // stage_floats = 32 (b_max + 1) floats: the inverses stay 128-byte aligned
-    stage.inv[0] = f + a.stage_nbuf * (int64_t)a.stage_floats;
+    stage.buf[1] = f + a.stage_floats;
+    stage.inv[0] = f + 2 * (int64_t)a.stage_floats;
     stage.inv[1] = stage.inv[0] + kPanel * kPanel;
     stage.bar = bars;
     stage.fail = &stage_fail;
     stage.pend = stage_pend;
     stage.extra = (uint32_t)a.stage_test_extra;
-    stage.nbuf = a.stage_nbuf;
     if (threadIdx.x == 0) {
       for (int k = 0; k < 4; ++k) {
         mbar_init(&bars[k], 1);
@@ -371,7 +370,7 @@ size_t gmres_smem(int m) { return sizeof(double) * ((size_t)(m + 1) * m + 4 * (s
 
 size_t gmres_smem_total(const SolverArgs& a) {
   return gmres_smem(a.m) + (a.x_in_smem ? sizeof(float) * (size_t)a.max_n : 0) +
-         (a.stage_floats > 0 ? 128 + sizeof(float) * (size_t)a.stage_nbuf * (size_t)a.stage_floats +
+         (a.stage_floats > 0 ? 128 + sizeof(float) * 2 * (size_t)a.stage_floats +
                                    sizeof(float) * 2 * kPanel * kPanel
                              : 0);
 }

@@ -36,7 +36,6 @@ struct SolverArgs {
   int max_n;             // largest simulation, in DOFs
   int stage_floats;      // > 0: band blocks staged in shared memory, floats per buffer (32 (b_max + 1))
   int stage_test_extra;  // > 0: the first forward block waits for bytes no copy delivers (tests the bounded wait)
-  int stage_nbuf;        // band-column stage buffers (1 or 2)
 };
 
 void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream_t s);

@@ -80,9 +80,7 @@ typedef struct {
   int32_t stage_band;                     /* 1: the triangular solves stream band blocks into shared memory
                                              with bulk asynchronous copies (same arithmetic, same results);
                                              2: as 1, but the first block's wait expects 16 bytes that no copy
-                                             delivers, so it runs out (tests EB_SIM_WAIT_TIMEOUT);
-                                             3: one band-column buffer instead of two (half the staging
-                                             memory; the copy then starts after the step that frees it) */
+                                             delivers, so it runs out (tests EB_SIM_WAIT_TIMEOUT) */
   int32_t warm_start;                     /* EB_WS_OFF | EB_WS_LEARNED (needs eb_ws_set_model) */
 } eb_params;
 
