@@ -188,6 +188,8 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     ph[k] ^= 1u;
   };
   const bool staged = st && !*st->fail;  // uniform: read after the barrier above
+  // the copies are issued by the CTA's last thread, off warp 0's chain
+  const bool issuer = threadIdx.x == blockDim.x - 1;
 
   for (int sweep = 0; sweep < 2; ++sweep) {
     const bool fwd = sweep == 0;
@@ -198,7 +200,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     }
     // block visited at step q (forward: q, backward: nblk - 1 - q)
     auto blk = [&](int q) { return fwd ? q : nblk - 1 - q; };
-    if (staged && threadIdx.x == 0 && !*st->fail) {
+    if (staged && issuer && !*st->fail) {
       issue_inv(blk(0), 0, fwd, fwd ? st->extra : 0u);
       if (nblk > 1) {
         issue_inv(blk(1), 1, fwd, 0u);
@@ -220,6 +222,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       if (staged) {
         if (q > 0) await((q - 1) & 1);
         if (warp == 0) await(2 + (q & 1));
+        else ph[2 + (q & 1)] ^= 1u;  // the other threads only follow the inverse barriers' phases
         if (!*st->fail) {
           if (q > 0) Pc = st->buf[(q - 1) & 1];
           Inv = st->inv[q & 1];
@@ -238,50 +241,72 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             int t = tlo;
             if (Pc) {
               const float* col = Pc + (i - pk0 - 1);
-              for (; t + 1 < pkb; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < pkb; t += 4) {
                 a0 = fmaf(col[t * (b - 1)], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * (b - 1)], yp[t + 1], a1);
+                a2 = fmaf(col[(t + 2) * (b - 1)], yp[t + 2], a2);
+                a3 = fmaf(col[(t + 3) * (b - 1)], yp[t + 3], a3);
               }
-              if (t < pkb) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+              for (; t < pkb; ++t) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             } else {
-              for (; t + 1 < pkb; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < pkb; t += 4) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
+                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              if (t < pkb) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              for (; t < pkb; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             }
           } else {  // U(i, pk0 + t), d = pk0 + t - i in [1, b]
             const int thi = min(pkb, i + b - pk0 + 1);
             int t = 0;
             if (Pc) {
               const float* col = Pc + (b - pk0 + i);
-              for (; t + 1 < thi; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < thi; t += 4) {
                 a0 = fmaf(col[t * b], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * b], yp[t + 1], a1);
+                a2 = fmaf(col[(t + 2) * b], yp[t + 2], a2);
+                a3 = fmaf(col[(t + 3) * b], yp[t + 3], a3);
               }
-              if (t < thi) a0 = fmaf(col[t * b], yp[t], a0);
+              for (; t < thi; ++t) a0 = fmaf(col[t * b], yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             } else {
-              for (; t + 1 < thi; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < thi; t += 4) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
+                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              if (t < thi) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              for (; t < thi; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             }
           }
           X(i) -= a0 + a1;
         }
         __syncwarp();
         // diagonal block: y = Inv x over the block's rows (two accumulators)
-        float d0 = 0.f, d1 = 0.f;
+        float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
         float* xb = &X(k0);
 #pragma unroll
-        for (int t = 0; t < kPanel; t += 2) {
+        for (int t = 0; t < kPanel; t += 4) {
           if (t < kb) d0 = fmaf(Inv[t * kPanel + lane], xb[t], d0);
           if (t + 1 < kb) d1 = fmaf(Inv[(t + 1) * kPanel + lane], xb[t + 1], d1);
+          if (t + 2 < kb) d2 = fmaf(Inv[(t + 2) * kPanel + lane], xb[t + 2], d2);
+          if (t + 3 < kb) d3 = fmaf(Inv[(t + 3) * kPanel + lane], xb[t + 3], d3);
         }
         __syncwarp();
         if (lane < kb) {
-          const float y = d0 + d1;
+          const float y = (d0 + d1) + (d2 + d3);
           xb[lane] = y;
           yb[q & 1][lane] = y;
           if (win) {  // the block is final: write it back, load the row that takes its slot
@@ -304,17 +329,27 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             int t = tlo;
             if (Pc) {
               const float* col = Pc + (i - pk0 - 1);
-              for (; t + 1 < pkb; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < pkb; t += 4) {
                 a0 = fmaf(col[t * (b - 1)], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * (b - 1)], yp[t + 1], a1);
+                a2 = fmaf(col[(t + 2) * (b - 1)], yp[t + 2], a2);
+                a3 = fmaf(col[(t + 3) * (b - 1)], yp[t + 3], a3);
               }
-              if (t < pkb) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+              for (; t < pkb; ++t) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             } else {
-              for (; t + 1 < pkb; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < pkb; t += 4) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
+                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              if (t < pkb) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              for (; t < pkb; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             }
             X(i) -= a0 + a1;
           }
@@ -326,17 +361,27 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             int t = 0;
             if (Pc) {
               const float* col = Pc + (b - pk0 + i);
-              for (; t + 1 < thi; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < thi; t += 4) {
                 a0 = fmaf(col[t * b], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * b], yp[t + 1], a1);
+                a2 = fmaf(col[(t + 2) * b], yp[t + 2], a2);
+                a3 = fmaf(col[(t + 3) * b], yp[t + 3], a3);
               }
-              if (t < thi) a0 = fmaf(col[t * b], yp[t], a0);
+              for (; t < thi; ++t) a0 = fmaf(col[t * b], yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             } else {
-              for (; t + 1 < thi; t += 2) {
+              float a2 = 0.f, a3 = 0.f;
+              for (; t + 3 < thi; t += 4) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
+                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
+                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              if (t < thi) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              for (; t < thi; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
+              a0 += a2;
+              a1 += a3;
             }
             X(i) -= a0 + a1;
           }
@@ -344,7 +389,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       }
       __syncthreads();
       // buffers freed at this step: band columns of block pj, inverse of block jb
-      if (staged && threadIdx.x == 0 && !*st->fail) {
+      if (staged && issuer && !*st->fail) {
         if (q + 1 <= nblk - 2) issue_cols(blk(q + 1), (q + 1) & 1, fwd);
         if (q + 2 <= nblk - 1) issue_inv(blk(q + 2), q & 1, fwd, 0u);
       }
