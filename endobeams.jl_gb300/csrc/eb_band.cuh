@@ -241,54 +241,34 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             int t = tlo;
             if (Pc) {
               const float* col = Pc + (i - pk0 - 1);
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < pkb; t += 4) {
+              for (; t + 1 < pkb; t += 2) {
                 a0 = fmaf(col[t * (b - 1)], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * (b - 1)], yp[t + 1], a1);
-                a2 = fmaf(col[(t + 2) * (b - 1)], yp[t + 2], a2);
-                a3 = fmaf(col[(t + 3) * (b - 1)], yp[t + 3], a3);
               }
-              for (; t < pkb; ++t) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < pkb) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
             } else {
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < pkb; t += 4) {
+              for (; t + 1 < pkb; t += 2) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
-                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
-                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              for (; t < pkb; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < pkb) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
             }
           } else {  // U(i, pk0 + t), d = pk0 + t - i in [1, b]
             const int thi = min(pkb, i + b - pk0 + 1);
             int t = 0;
             if (Pc) {
               const float* col = Pc + (b - pk0 + i);
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < thi; t += 4) {
+              for (; t + 1 < thi; t += 2) {
                 a0 = fmaf(col[t * b], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * b], yp[t + 1], a1);
-                a2 = fmaf(col[(t + 2) * b], yp[t + 2], a2);
-                a3 = fmaf(col[(t + 3) * b], yp[t + 3], a3);
               }
-              for (; t < thi; ++t) a0 = fmaf(col[t * b], yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < thi) a0 = fmaf(col[t * b], yp[t], a0);
             } else {
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < thi; t += 4) {
+              for (; t + 1 < thi; t += 2) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
-                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
-                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              for (; t < thi; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < thi) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
             }
           }
           X(i) -= a0 + a1;
@@ -329,27 +309,17 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             int t = tlo;
             if (Pc) {
               const float* col = Pc + (i - pk0 - 1);
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < pkb; t += 4) {
+              for (; t + 1 < pkb; t += 2) {
                 a0 = fmaf(col[t * (b - 1)], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * (b - 1)], yp[t + 1], a1);
-                a2 = fmaf(col[(t + 2) * (b - 1)], yp[t + 2], a2);
-                a3 = fmaf(col[(t + 3) * (b - 1)], yp[t + 3], a3);
               }
-              for (; t < pkb; ++t) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < pkb) a0 = fmaf(col[t * (b - 1)], yp[t], a0);
             } else {
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < pkb; t += 4) {
+              for (; t + 1 < pkb; t += 2) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
-                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
-                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              for (; t < pkb; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < pkb) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
             }
             X(i) -= a0 + a1;
           }
@@ -361,27 +331,17 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             int t = 0;
             if (Pc) {
               const float* col = Pc + (b - pk0 + i);
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < thi; t += 4) {
+              for (; t + 1 < thi; t += 2) {
                 a0 = fmaf(col[t * b], yp[t], a0);
                 a1 = fmaf(col[(t + 1) * b], yp[t + 1], a1);
-                a2 = fmaf(col[(t + 2) * b], yp[t + 2], a2);
-                a3 = fmaf(col[(t + 3) * b], yp[t + 3], a3);
               }
-              for (; t < thi; ++t) a0 = fmaf(col[t * b], yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < thi) a0 = fmaf(col[t * b], yp[t], a0);
             } else {
-              float a2 = 0.f, a3 = 0.f;
-              for (; t + 3 < thi; t += 4) {
+              for (; t + 1 < thi; t += 2) {
                 a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
                 a1 = fmaf(V.at(i, pk0 + t + 1), yp[t + 1], a1);
-                a2 = fmaf(V.at(i, pk0 + t + 2), yp[t + 2], a2);
-                a3 = fmaf(V.at(i, pk0 + t + 3), yp[t + 3], a3);
               }
-              for (; t < thi; ++t) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
-              a0 += a2;
-              a1 += a3;
+              if (t < thi) a0 = fmaf(V.at(i, pk0 + t), yp[t], a0);
             }
             X(i) -= a0 + a1;
           }
