@@ -46,9 +46,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # FP64 floating-point operations the device beam kernel executes per element
-# evaluation: 202 DADD + 368 DMUL + 714 DFMA counted by ncu's SASS counters on
-# k_beam (profiles/beam_kernel_nets16.md).
-F_ELEM_FP64 = 1998.0
+# evaluation: 1,702 DADD + 3,085 DMUL + 5,987 DFMA (FMA = 2) counted by ncu's
+# SASS counters on a launch in which every element of a 48-wire stent is
+# evaluated (profiles/beam_kernel_stent.md).
+F_ELEM_FP64 = 1702.0 + 3085.0 + 2 * 5987.0
 
 METRIC = "HHT steps/s & Newton iters/step, batched+learned vs plain"
 MODEL = os.path.join(ROOT, "endobeams.jl_gb300", "models", "warm_start_stents.npz")
@@ -259,9 +260,10 @@ class ClockSampler:
 class Driver:
     """The batched time loop of run_simulation! (per-simulation Δt halving and rollback)."""
 
-    def __init__(self, eng, params):
+    def __init__(self, eng, params, elems=None):
         self.eng = eng
         self.p = params
+        self.elems = np.asarray(elems if elems is not None else np.zeros(eng.n), np.int64)
         self.S = eng.n
         self.t = np.zeros(self.S)
         self.dt = np.full(self.S, params.initial_timestep)
@@ -274,6 +276,7 @@ class Driver:
         self.batch_iters = 0
         self.ws_used = 0
         self.ws_steps = 0
+        self.elem_evals = 0
 
     def step(self, e2e=False, ubuf=None):
         eng = self.eng
@@ -284,6 +287,8 @@ class Driver:
         self.newton += sum(s["newton_iterations"] for s in st)
         self.batch_iters += max(s["newton_iterations"] for s in st)
         self.krylov += sum(s["krylov_iterations"] for s in st)
+        # element evaluations of the corrector iterations (one k_beam pass per iteration of each sim)
+        self.elem_evals += int(sum(int(e) * s["newton_iterations"] for e, s in zip(self.elems, st)))
         self.ws_used += sum(s["warm_start_used"] for s in st)
         self.ws_steps += len(st)
         failed = k > self.p.max_iterations
@@ -313,7 +318,7 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
         from endobeams_gb300 import warm_start as W
         eng.set_warm_start(W.WarmStartModel.load(MODEL))
     mem, band_sims = eng.memory()
-    drv = Driver(eng, params)
+    drv = Driver(eng, params, [len(c.beams) for c in confs])
     for _ in range(args.warmup):
         drv.step()
     eng.phase_times(reset=True)
@@ -326,6 +331,7 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
     phase_ms, launches = eng.phase_times(reset=True)
     out = {"sim_steps": drv.ok_steps, "ms": ms, "newton": drv.newton, "krylov": drv.krylov,
            "ws_used": drv.ws_used, "ws_steps": drv.ws_steps, "phase_ms": phase_ms, "launches": launches,
+           "elem_evals": drv.elem_evals,
            "nodes": sum(len(c.nodes) for c in confs), "elements": sum(len(c.beams) for c in confs),
            "sims": len(idx), "device_bytes": mem, "band_sims": band_sims, "e2e": None}
     if e2e and not args.no_e2e:
@@ -385,7 +391,7 @@ def gpu_arm(args, rank, world):
             tot["device_bytes_max"] = r["device_bytes"]
         else:
             for k in ("sim_steps", "ms", "newton", "krylov", "ws_used", "ws_steps", "nodes", "elements", "sims",
-                      "band_sims"):
+                      "band_sims", "elem_evals"):
                 tot[k] += r[k]
             tot["device_bytes_max"] = max(tot["device_bytes_max"], r["device_bytes"])
             for k in tot["phase_ms"]:
@@ -408,9 +414,10 @@ def gpu_arm(args, rank, world):
     # ---- rooflines: the element kernel (FP64 pipe) and the Krylov kernel (HBM)
     peak_fp64 = eb.fp64_peak_tflops()
     rooflines = {}
-    if launches["beam"]:
+    if launches["beam"] and tot["elem_evals"]:
+        # FP64 flops of every element evaluation of the timed corrector iterations over the phase's device time
         avg_beam_ms = phase_ms["beam"] / launches["beam"]
-        ach = F_ELEM_FP64 * tot["elements"] / len(groups) / (avg_beam_ms * 1e-3) / 1e12
+        ach = F_ELEM_FP64 * tot["elem_evals"] / (phase_ms["beam"] * 1e-3) / 1e12
         rooflines["beam"] = {"kernel": "k_beam (corotational element, FP64)", "bound": "fp64", "achieved": ach,
                              "peak": peak_fp64, "peak_source": "measured (eb_fp64_peak FMA probe on this GPU)",
                              "unit": "TFLOP/s", "frac": ach / peak_fp64, "traffic": None,
