@@ -36,7 +36,7 @@ class EbParams(C.Structure):
         ("linear_tol", C.c_double), ("inner_tol", C.c_double),
         ("max_refinements", C.c_int32), ("threads_per_sim", C.c_int32), ("timing", C.c_int32),
         ("preconditioner", C.c_int32), ("refactor_its", C.c_int32), ("stage_band", C.c_int32),
-        ("warm_start", C.c_int32),
+        ("warm_start", C.c_int32), ("use_graph", C.c_int32),
     ]
 
 

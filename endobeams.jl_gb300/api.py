@@ -262,6 +262,7 @@ class SimulationParams:
     stage_band: int = 1              # 1: stream band blocks into shared memory with bulk async copies; 0: off;
                                      # 2: test of the bounded wait (the first block's wait runs out)
     warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start)
+    use_graph: bool = True           # replay each Newton iteration from a CUDA graph
 
     def to_c(self) -> _lib.EbParams:
         p = _lib.default_params()
@@ -285,6 +286,7 @@ class SimulationParams:
         if self.warm_start not in ("off", "learned"):
             raise ValueError("warm_start must be 'off' or 'learned'")
         p.warm_start = 1 if self.warm_start == "learned" else 0
+        p.use_graph = int(bool(self.use_graph))
         return p
 
 

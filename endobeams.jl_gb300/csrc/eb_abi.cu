@@ -293,9 +293,22 @@ struct WsHost {
   }
 };
 
+// A captured corrector iteration (see record_iteration) and its own timer events.
+struct IterGraph {
+  cudaGraphExec_t exec = nullptr;
+  uint64_t gen = 0;
+  bool timer_ready = false;
+  PhaseTimer timer;  // events recorded by the graph; launch counts per replay
+};
+
 struct eb_handle {
   PhaseTimer timer;
   WsHost ws;
+  // pinned host mirrors used by the captured iterations, and the graphs
+  int *pin_active = nullptr, *pin_refactor = nullptr;
+  double* pin_norms = nullptr;
+  IterGraph graph[2];      // without / with band refactorisation
+  uint64_t graph_gen = 1;  // bumped when launch parameters captured in the graphs change
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   eb_params P;
   int n_sims = 0;
@@ -365,41 +378,135 @@ int upload_mask(eb_handle* h, int* dst, const int32_t* mask) {
 
 // Linear solve of the simulations active on the device; `mask` (host, n_sims)
 // marks the same simulations for the refactorisation decision.
-int solve(eb_handle* h, const int* mask) {
+// Host part of a linear solve: which simulations refactorise their band
+// (factors missing, stale because Δt changed, or slow: too many GMRES
+// iterations); fills refactor_mask.
+bool plan_refactor(eb_handle* h, const int* mask) {
+  bool any = false;
+  if (!h->any_band) return false;
+  for (int s = 0; s < h->n_sims; ++s) {
+    int r = 0;
+    if (mask[s] && h->band_b[s] > 0)
+      r = h->need_refactor[s] || h->dt_at_factor[s] != h->cur_dt[s] || h->P.refactor_its <= 0;
+    h->refactor_mask[s] = r;
+    if (r) {
+      h->need_refactor[s] = 0;
+      h->dt_at_factor[s] = h->cur_dt[s];
+      ++h->factorizations;
+      any = true;
+    }
+  }
+  return any;
+}
+
+// Stream part of a linear solve; `refactor_src` is the host copy of the refactor mask
+// (pinned when the launches are captured into a graph).
+int launch_solve(eb_handle* h, bool refactor, const int* refactor_src, PhaseTimer& T) {
   if (h->any_jacobi) {
     launch_block_jacobi(h->d, h->d_Dinv64, h->d_Dinv32, h->stream);
-    h->timer.launches[EB_PHASE_PRECOND] += 1;
+    T.launches[EB_PHASE_PRECOND] += 1;
   }
-  if (h->any_band) {
-    // refactorise the simulations whose factors are missing, stale (Δt changed) or slow (GMRES iterations)
-    bool any = false;
-    for (int s = 0; s < h->n_sims; ++s) {
-      int r = 0;
-      if (mask[s] && h->band_b[s] > 0)
-        r = h->need_refactor[s] || h->dt_at_factor[s] != h->cur_dt[s] || h->P.refactor_its <= 0;
-      h->refactor_mask[s] = r;
-      if (r) {
-        h->need_refactor[s] = 0;
-        h->dt_at_factor[s] = h->cur_dt[s];
-        ++h->factorizations;
-        any = true;
-      }
-    }
-    if (any) {
-      CK(cudaMemcpyAsync(h->d_refactor, h->refactor_mask.data(), sizeof(int) * h->n_sims, cudaMemcpyHostToDevice,
-                         h->stream));
-      launch_band_fill(h->d, h->band, h->d_blk_row, h->stream);
-      CK(launch_band_lu(h->d, h->band, h->max_b, h->stream));
-      h->timer.launches[EB_PHASE_PRECOND] += 3;
-    }
+  if (refactor) {
+    CK(cudaMemcpyAsync(h->d_refactor, refactor_src, sizeof(int) * h->n_sims, cudaMemcpyHostToDevice, h->stream));
+    launch_band_fill(h->d, h->band, h->d_blk_row, h->stream);
+    CK(launch_band_lu(h->d, h->band, h->max_b, h->stream));
+    T.launches[EB_PHASE_PRECOND] += 3;
   }
   CK(cudaGetLastError());
-  h->timer.mark(EB_PHASE_PRECOND, h->stream);
+  T.mark(EB_PHASE_PRECOND, h->stream);
   const bool fp32 = h->P.precision == EB_PREC_MIXED;
   int threads = h->P.threads_per_sim > 0 ? h->P.threads_per_sim : 256;
   CK(launch_gmres(h->sa, fp32, threads, h->stream));
-  h->timer.mark(EB_PHASE_KRYLOV, h->stream);
-  h->timer.launches[EB_PHASE_KRYLOV] += 1;
+  T.mark(EB_PHASE_KRYLOV, h->stream);
+  T.launches[EB_PHASE_KRYLOV] += 1;
+  return EB_OK;
+}
+
+int solve(eb_handle* h, const int* mask) {
+  const bool any = plan_refactor(h, mask);
+  return launch_solve(h, any, h->refactor_mask.data(), h->timer);
+}
+
+int record_iteration(eb_handle* h, bool refactor, PhaseTimer& T);
+
+// Launches the captured corrector iteration (capturing it on first use).
+int run_iteration_graph(eb_handle* h, bool refactor) {
+  IterGraph& G = h->graph[refactor ? 1 : 0];
+  if (!G.exec || G.gen != h->graph_gen) {
+    if (G.exec) {
+      cudaGraphExecDestroy(G.exec);
+      G.exec = nullptr;
+    }
+    if (!G.timer_ready) {
+      G.timer.init(h->P.timing != 0);
+      G.timer_ready = true;
+    }
+    G.timer.used = 0;
+    for (int k = 0; k < EB_NPHASES; ++k) G.timer.launches[k] = 0;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
+    const int rc = record_iteration(h, refactor, G.timer);
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CK(e);
+    const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ei);
+    G.gen = h->graph_gen;
+  }
+  CK(cudaGraphLaunch(G.exec, h->stream));
+  for (int k = 0; k < EB_NPHASES; ++k) h->timer.launches[k] += G.timer.launches[k];
+  return EB_OK;
+}
+
+// After a replay has completed: its phase times into the handle's totals.
+void resolve_graph_times(eb_handle* h, bool refactor) {
+  IterGraph& G = h->graph[refactor ? 1 : 0];
+  if (!G.timer.on) return;
+  for (int i = 1; i < G.timer.used; ++i) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, G.timer.pool[i - 1], G.timer.pool[i]) == cudaSuccess)
+      h->timer.ms[G.timer.phase_of[i]] += t;
+  }
+}
+
+// One corrector iteration after the first (assembly, residual, solve, Newmark
+// and rotation updates, norms) as stream operations; eb_step replays it from
+// a CUDA graph, one per refactorisation variant.  Its host inputs and outputs
+// (mask of running simulations, refactor mask, Newton norms) are pinned.
+int record_iteration(eb_handle* h, bool refactor, PhaseTimer& T) {
+  const Dev& d = h->d;
+  cudaStream_t st = h->stream;
+  const double a = h->P.alpha, b = h->P.beta, g = h->P.gamma;
+  const int S = h->n_sims;
+  T.begin(st);
+  CK(cudaMemcpyAsync(h->d_active, h->pin_active, sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  T.mark(EB_PHASE_UPDATE, st);
+  launch_beam(d, h->gauss, st);
+  T.mark(EB_PHASE_BEAM, st);
+  T.launches[EB_PHASE_BEAM] += 1;
+  if (h->any_contact) {
+    launch_contact(d, h->gauss, st);
+    T.mark(EB_PHASE_CONTACT, st);
+    T.launches[EB_PHASE_CONTACT] += 1;
+  }
+  launch_gather(d, a, h->any_contact, st);
+  T.mark(EB_PHASE_ASSEMBLY, st);
+  T.launches[EB_PHASE_ASSEMBLY] += 2;
+  launch_corrector_rhs(d, a, st);
+  launch_apply_bc(d, st);
+  T.mark(EB_PHASE_RESIDUAL, st);
+  T.launches[EB_PHASE_RESIDUAL] += 3;
+  int rc = launch_solve(h, refactor, h->pin_refactor, T);
+  if (rc) return rc;
+  launch_global_corrector(d, st);
+  launch_local_corrector(d, b, g, st);
+  T.launches[EB_PHASE_UPDATE] += 2;
+  CK(cudaMemcpyAsync(h->pin_norms, h->d_norms, sizeof(double) * 5 * S, cudaMemcpyDeviceToHost, st));
+  T.mark(EB_PHASE_UPDATE, st);
   return EB_OK;
 }
 
@@ -432,6 +539,7 @@ int eb_default_params(eb_params* p) {
   p->refactor_its = 16;
   p->stage_band = 1;
   p->warm_start = EB_WS_OFF;
+  p->use_graph = 1;
   return EB_OK;
 }
 
@@ -489,6 +597,9 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   CK(cudaEventCreate(&h->t0));
   CK(cudaEventCreate(&h->t1));
   h->timer.init(p->timing != 0);
+  CK(cudaMallocHost(&h->pin_active, sizeof(int) * (size_t)n_sims));
+  CK(cudaMallocHost(&h->pin_refactor, sizeof(int) * (size_t)n_sims));
+  CK(cudaMallocHost(&h->pin_norms, sizeof(double) * 5 * (size_t)n_sims));
 
   // ---- sizes and offsets
   h->node_off.assign(n_sims + 1, 0);
@@ -966,6 +1077,13 @@ int eb_destroy(eb_handle* h) {
     cudaStreamDestroy(h->stream);
   }
   h->timer.destroy();
+  for (auto& G : h->graph) {
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    G.timer.destroy();
+  }
+  if (h->pin_active) cudaFreeHost(h->pin_active);
+  if (h->pin_refactor) cudaFreeHost(h->pin_refactor);
+  if (h->pin_norms) cudaFreeHost(h->pin_norms);
   if (h->t0) cudaEventDestroy(h->t0);
   if (h->t1) cudaEventDestroy(h->t1);
   delete h;
@@ -1202,6 +1320,19 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     bool any = false;
     for (int s = 0; s < S; ++s) any |= running[s] != 0;
     if (!any) break;
+    if (P.use_graph && !(learned && first)) {
+      // the iteration as one CUDA graph launch (the learned start's first iteration, with its
+      // host-side check, runs as separate launches)
+      std::memcpy(h->pin_active, running.data(), sizeof(int) * S);
+      const bool ref = plan_refactor(h, running.data());
+      if (ref) std::memcpy(h->pin_refactor, h->refactor_mask.data(), sizeof(int) * S);
+      rc = run_iteration_graph(h, ref);
+      if (rc) return rc;
+      CK(cudaStreamSynchronize(st));
+      resolve_graph_times(h, ref);
+      std::memcpy(h->h_norms.data(), h->pin_norms, sizeof(double) * 5 * S);
+      first = false;
+    } else {
     T.begin(st);
     CK(cudaMemcpyAsync(h->d_active, running.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
     T.mark(EB_PHASE_UPDATE, st);
@@ -1234,6 +1365,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     T.mark(EB_PHASE_UPDATE, st);
     CK(cudaStreamSynchronize(st));
     T.resolve();
+    }
     for (int s = 0; s < S; ++s) {
       if (!running[s]) continue;
       const double* q = &h->h_norms[5 * s];
@@ -1241,6 +1373,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
         // a bulk-copy wait ran out in this solve: stop this simulation's Newton loop (the step
         // reports EB_SIM_WAIT_TIMEOUT) and read band blocks from global memory from now on
         h->sa.stage_floats = 0;
+        h->graph_gen += 1;
         running[s] = 0;
         k[s] = P.max_iterations + 1;
         continue;
@@ -1277,6 +1410,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
       // and read band blocks from global memory from now on
       k[s] = P.max_iterations + 1;
       h->sa.stage_floats = 0;
+      h->graph_gen += 1;
     }
     q.newton_iterations = iter[s];
     q.krylov_iterations = its[s];

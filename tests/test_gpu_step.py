@@ -162,3 +162,16 @@ def test_stent_population_batch_matches_single(eb, scenes):
     eb.run_simulations([b[0] for b in built], p, [b[2] for b in built], max_steps=3)
     for b, u in zip(built, singles):
         assert np.array_equal(b[0].nodes.un, u)
+
+
+def test_graph_replay_matches_direct_launches(eb, scenes):
+    """Newton iterations replayed from a CUDA graph give the same bits as the
+    same launches issued one by one."""
+    out = {}
+    for graph in (True, False):
+        conf, p, inter = scenes.ring_drop(steps=20)
+        p.tolerance_residual = 1e-5
+        p.use_graph = graph
+        res = eb.run_simulation(conf, p, inter)
+        out[graph] = (conf.nodes.un.copy(), res.ks[0])
+    assert np.array_equal(out[True][0], out[False][0]) and out[True][1] == out[False][1]
