@@ -791,7 +791,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   std::vector<int> pos_all(NN), node_at(NN);
   std::vector<int64_t> band_off(n_sims + 1, 0);
   h->band_b.assign(n_sims, 0);
-  const int bmax = ((227 * 1024) / 4 / kPanel - kPanel) / 2;  // shared-memory limit of k_band_lu
+  const int bmax = (((227 * 1024) / 4 - 8) / kPanel - kPanel) / 2;  // shared-memory limit of k_band_lu
   for (int s = 0; s < n_sims; ++s) {
     const int64_t no = h->node_off[s], n = h->node_off[s + 1] - no;
     std::vector<std::vector<int>> la(n);

@@ -140,35 +140,48 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
     // row (broadcast) and update consecutive band entries (coalesced).
     // The tile's band entries are loaded before the product loop so their global-memory
     // latency overlaps the FMAs.
+    // Rows and columns past q are read from shared memory without guards (the
+    // allocation is padded) and their products discarded.
     const int R = (q + 7) >> 3;
     for (int tile = threadIdx.x; tile < R * R; tile += kLuThreads) {
       const int ti = tile % R, tj = tile / R;
+      unsigned rv = 0u, cv = 0u;  // valid rows / columns of the tile
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        rv |= (ti + a * R < q ? 1u : 0u) << a;
+        cv |= (tj + a * R < q ? 1u : 0u) << a;
+      }
       float acc[8][8], old[8][8];
 #pragma unroll
       for (int c = 0; c < 8; ++c)
 #pragma unroll
         for (int a = 0; a < 8; ++a)
-          old[a][c] = (ti + a * R < q && tj + c * R < q) ? V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) : 0.f;
+          old[a][c] = ((rv >> a) & (cv >> c) & 1u) ? V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) : 0.f;
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int c = 0; c < 8; ++c) acc[a][c] = 0.f;
+      const float* pp = P + kb + ti;  // row ti + a R of column t at pp[a R + ldp t]
+      const float* up = U + tj;       // column tj + c R of row t at up[c R + b t]
+#pragma unroll 2
       for (int t = 0; t < kb; ++t) {
         float l[8], u[8];
 #pragma unroll
-        for (int a = 0; a < 8; ++a) l[a] = (ti + a * R < q) ? P[(kb + ti + a * R) + ldp * t] : 0.f;
+        for (int a = 0; a < 8; ++a) l[a] = pp[a * R];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) u[c] = (tj + c * R < q) ? U[t * b + tj + c * R] : 0.f;
+        for (int c = 0; c < 8; ++c) u[c] = up[c * R];
 #pragma unroll
         for (int a = 0; a < 8; ++a)
 #pragma unroll
           for (int c = 0; c < 8; ++c) acc[a][c] = fmaf(l[a], u[c], acc[a][c]);
+        pp += ldp;
+        up += b;
       }
 #pragma unroll
       for (int c = 0; c < 8; ++c)
 #pragma unroll
         for (int a = 0; a < 8; ++a)
-          if (ti + a * R < q && tj + c * R < q) V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) = old[a][c] - acc[a][c];
+          if ((rv >> a) & (cv >> c) & 1u) V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) = old[a][c] - acc[a][c];
     }
     // ---- write back panel and U12
     if (lane < kb)
@@ -187,7 +200,8 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
 
 cudaError_t launch_band_lu(const Dev& d, const BandDev& B, int max_b, cudaStream_t s) {
   if (max_b <= 0) return cudaSuccess;
-  const size_t smem = sizeof(float) * (size_t)kPanel * (kPanel + 2 * (size_t)max_b);
+  // panel, U12 and 8 floats of padding for the unguarded reads past q
+  const size_t smem = sizeof(float) * ((size_t)kPanel * (kPanel + 2 * (size_t)max_b) + 8);
   cudaError_t e = cudaFuncSetAttribute(k_band_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_band_lu<<<d.n_sims, kLuThreads, smem, s>>>(d, B);
