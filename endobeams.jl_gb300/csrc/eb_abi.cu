@@ -1320,9 +1320,9 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     bool any = false;
     for (int s = 0; s < S; ++s) any |= running[s] != 0;
     if (!any) break;
-    if (P.use_graph && !(learned && first)) {
+    if (P.use_graph && !P.timing && !(learned && first)) {
       // the iteration as one CUDA graph launch (the learned start's first iteration, with its
-      // host-side check, runs as separate launches)
+      // host-side check, and iterations timed phase by phase run as separate launches)
       std::memcpy(h->pin_active, running.data(), sizeof(int) * S);
       const bool ref = plan_refactor(h, running.data());
       if (ref) std::memcpy(h->pin_refactor, h->refactor_mask.data(), sizeof(int) * S);

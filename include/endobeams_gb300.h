@@ -82,8 +82,9 @@ typedef struct {
                                              2: as 1, but the first block's wait expects 16 bytes that no copy
                                              delivers, so it runs out (tests EB_SIM_WAIT_TIMEOUT) */
   int32_t warm_start;                     /* EB_WS_OFF | EB_WS_LEARNED (needs eb_ws_set_model) */
-  int32_t use_graph;                      /* 1: each Newton iteration after the first is one CUDA graph
-                                             launch (captured once per handle and refactorisation variant) */
+  int32_t use_graph;                      /* 1: each Newton iteration is one CUDA graph launch (captured once
+                                             per handle and refactorisation variant); not with timing = 1,
+                                             whose per-phase events need separate launches */
 } eb_params;
 
 /* Newton start of each step */

@@ -167,11 +167,13 @@ def test_stent_population_batch_matches_single(eb, scenes):
 def test_graph_replay_matches_direct_launches(eb, scenes):
     """Newton iterations replayed from a CUDA graph give the same bits as the
     same launches issued one by one."""
-    out = {}
-    for graph in (True, False):
-        conf, p, inter = scenes.ring_drop(steps=20)
-        p.tolerance_residual = 1e-5
-        p.use_graph = graph
-        res = eb.run_simulation(conf, p, inter)
-        out[graph] = (conf.nodes.un.copy(), res.ks[0])
-    assert np.array_equal(out[True][0], out[False][0]) and out[True][1] == out[False][1]
+    for refactor_its in (16, 0):  # 0: the band is refactorised inside every captured iteration
+        out = {}
+        for graph in (True, False):
+            conf, p, inter = scenes.ring_drop(steps=20)
+            p.tolerance_residual = 1e-5
+            p.refactor_its = refactor_its
+            p.use_graph = graph
+            res = eb.run_simulation(conf, p, inter)
+            out[graph] = (conf.nodes.un.copy(), res.ks[0])
+        assert np.array_equal(out[True][0], out[False][0]) and out[True][1] == out[False][1]
