@@ -202,6 +202,20 @@ int rcm_order(const std::vector<std::vector<int>>& adj, std::vector<int>& pos) {
   return bw;
 }
 
+// The samples (sign flipped when `negate`) in the interior of the zero-padded
+// coefficient layout; the device prefilter completes it.
+std::vector<double> sdf_padded(const double* values, const int64_t dims[3], bool negate) {
+  const int64_t px = dims[0] + 2, py = dims[1] + 2, pz = dims[2] + 2;
+  std::vector<double> c((size_t)(px * py * pz), 0.0);
+  for (int64_t k = 0; k < dims[2]; ++k)
+    for (int64_t j = 0; j < dims[1]; ++j)
+      for (int64_t i = 0; i < dims[0]; ++i) {
+        double v = values[i + dims[0] * (j + dims[1] * k)];
+        c[(size_t)((i + 1) + px * ((j + 1) + py * (k + 1)))] = negate ? -v : v;
+      }
+  return c;
+}
+
 std::vector<double> sdf_coefficients(const double* values, const int64_t dims[3], bool negate) {
   const int64_t px = dims[0] + 2, py = dims[1] + 2, pz = dims[2] + 2;
   std::vector<double> c((size_t)(px * py * pz), 0.0);
@@ -860,15 +874,19 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
       for (size_t i = c0; i < c1; ++i)
         pool.emplace_back([&, i] {
           const eb_sim_desc& S = sims[todo[i]];
-          chunk[i - c0] = sdf_coefficients(S.sdf_values, S.sdf_dims, S.sdf_inside == 0);
+          chunk[i - c0] = sdf_padded(S.sdf_values, S.sdf_dims, S.sdf_inside == 0);
         });
       for (auto& th : pool) th.join();
       for (size_t i = c0; i < c1; ++i) {
+        const eb_sim_desc& S = sims[todo[i]];
         double* c;
         CK(A.upload(&c, chunk[i - c0]));
+        launch_sdf_prefilter(c, (int)S.sdf_dims[0], (int)S.sdf_dims[1], (int)S.sdf_dims[2], h->stream);
+        CK(cudaGetLastError());
         surf[todo[i]].coef = c;
         std::vector<double>().swap(chunk[i - c0]);
       }
+      CK(cudaStreamSynchronize(h->stream));
     }
     for (int s : sdf_sims) surf[s].coef = surf[owner[s]].coef;
   }

@@ -104,5 +104,7 @@ void launch_local_corrector(const Dev& d, double beta, double gamma, cudaStream_
 void launch_commit(const Dev& d, const int* mask, bool commit, cudaStream_t s);
 // node state at n+1 <- node state at n (the node part of update_not_converged!)
 void launch_restore_nodes(const Dev& d, const int* mask, cudaStream_t s);
+// quadratic B-spline prefilter of a padded SDF coefficient grid (interior = samples), eb_testing.cu
+void launch_sdf_prefilter(double* coef, int nx, int ny, int nz, cudaStream_t s);
 
 }  // namespace eb

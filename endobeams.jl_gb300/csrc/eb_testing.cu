@@ -200,6 +200,17 @@ __global__ void k_sdf_prefilter_axis(double* c, int nx, int ny, int nz, int axis
 
 }  // namespace
 
+// Prefilters a padded coefficient grid whose interior holds the SDF samples
+// (three passes, one thread per grid line).
+namespace eb {
+void launch_sdf_prefilter(double* coef, int nx, int ny, int nz, cudaStream_t st) {
+  const int64_t px = nx + 2, py = ny + 2;
+  k_sdf_prefilter_axis<<<(unsigned)(((int64_t)ny * nz + 127) / 128), 128, 0, st>>>(coef, nx, ny, nz, 0);
+  k_sdf_prefilter_axis<<<(unsigned)((px * nz + 127) / 128), 128, 0, st>>>(coef, nx, ny, nz, 1);
+  k_sdf_prefilter_axis<<<(unsigned)((px * py + 127) / 128), 128, 0, st>>>(coef, nx, ny, nz, 2);
+}
+}  // namespace eb
+
 extern "C" int eb_contact_eval_noalloc(int64_t n, const double* d_in, const double* gauss6, const double* props,
                                        const double* surf, const double* d_sdf_values, double* d_out,
                                        int32_t* d_flags, void* stream) {
