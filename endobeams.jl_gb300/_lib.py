@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libendobeams_gb300.so")
 EB_OK = 0
 EB_PREC_FP64 = 0
 EB_PREC_MIXED = 1
-EB_SURFACE_NONE, EB_SURFACE_SPHERE, EB_SURFACE_SDF = 0, 1, 2
+EB_SURFACE_NONE, EB_SURFACE_SPHERE, EB_SURFACE_SDF, EB_SURFACE_PLANE = 0, 1, 2, 3
 SIM_STATUS = {0: "OK", 1: "NOT_CONVERGED", 2: "NAN", 3: "KRYLOV_STAGNATED"}
 
 P_d = C.POINTER(C.c_double)
@@ -54,6 +54,7 @@ class EbSimDesc(C.Structure):
         ("sphere_center", C.c_double * 3), ("sphere_radius", C.c_double),
         ("sdf_dims", C.c_int64 * 3), ("sdf_origin", C.c_double * 3), ("sdf_spacing", C.c_double * 3),
         ("sdf_values", P_d), ("sdf_inside", C.c_int32),
+        ("plane_axis", C.c_int32), ("plane_position", C.c_double),
     ]
 
 

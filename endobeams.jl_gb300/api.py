@@ -158,9 +158,22 @@ class SphereSurface:
 
 @dataclass
 class PlaneSurface:
-    """Declared by the reference (def_interactions.jl:24-27) without a gap method; not usable there either."""
+    """PlaneSurface(position, axis) (def_interactions.jl:24-27): the plane x[axis] = position.
+
+    The reference declares it without a gap function.  Here the body lies on
+    the positive side: gap = x[axis] - position - r, normal e_axis, zero
+    curvature (the sphere's convention, utils_compute_interactions_beams.jl:2-36)."""
     position: float
-    axis: str
+    axis: str  # 'x', 'y' or 'z'
+
+    @property
+    def axis_index(self) -> int:
+        a = self.axis
+        if isinstance(a, str) and a.lower() in ("x", "y", "z"):
+            return "xyz".index(a.lower())
+        if isinstance(a, (int, np.integer)) and 0 <= int(a) <= 2:
+            return int(a)
+        raise ValueError(f"PlaneSurface.axis must be 'x', 'y' or 'z', got {a!r}")
 
 
 class DiscreteSignedDistanceField:
@@ -350,6 +363,10 @@ class GpuSimulations:
                 for i in range(3):
                     d.sphere_center[i] = float(m.center[i])
                 d.sphere_radius = float(m.radius)
+            elif isinstance(m, PlaneSurface):
+                d.surface = _lib.EB_SURFACE_PLANE
+                d.plane_axis = m.axis_index
+                d.plane_position = float(m.position)
             elif isinstance(m, DiscreteSignedDistanceField):
                 d.surface = _lib.EB_SURFACE_SDF
                 for i in range(3):

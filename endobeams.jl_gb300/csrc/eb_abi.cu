@@ -632,6 +632,10 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
       if (S.fixed_dofs[k] < 0 || S.fixed_dofs[k] >= 6 * S.n_nodes) return fail(EB_ERR_ARG, "sim %d: fixed dof out of range", s);
     for (int64_t k = 0; k < S.n_loaded; ++k)
       if (S.loaded_dofs[k] < 0 || S.loaded_dofs[k] >= 6 * S.n_nodes) return fail(EB_ERR_ARG, "sim %d: loaded dof out of range", s);
+    if (S.surface < EB_SURFACE_NONE || S.surface > EB_SURFACE_PLANE)
+      return fail(EB_ERR_ARG, "sim %d: unknown surface kind %d", s, (int)S.surface);
+    if (S.surface == EB_SURFACE_PLANE && (S.plane_axis < 0 || S.plane_axis > 2))
+      return fail(EB_ERR_ARG, "sim %d: plane_axis must be 0, 1 or 2", s);
     if (S.surface == EB_SURFACE_SDF) {
       if (!S.sdf_values || S.sdf_dims[0] < 1 || S.sdf_dims[1] < 1 || S.sdf_dims[2] < 1)
         return fail(EB_ERR_ARG, "sim %d: SDF grid missing", s);
@@ -724,7 +728,11 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
         sf.kind = 0;
         sf.cx = S.sphere_center[0]; sf.cy = S.sphere_center[1]; sf.cz = S.sphere_center[2];
         sf.R = S.sphere_radius;
-      } else {
+      } else if (S.surface == EB_SURFACE_PLANE) {
+        sf.kind = 2;
+        sf.axis = S.plane_axis;
+        sf.pos = S.plane_position;
+      } else if (S.surface == EB_SURFACE_SDF) {
         sf.kind = 1;
         sf.nx = (int)S.sdf_dims[0]; sf.ny = (int)S.sdf_dims[1]; sf.nz = (int)S.sdf_dims[2];
         sf.x0 = S.sdf_origin[0]; sf.y0 = S.sdf_origin[1]; sf.z0 = S.sdf_origin[2];

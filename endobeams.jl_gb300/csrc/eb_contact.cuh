@@ -16,10 +16,13 @@ struct ContactProps {
   double kn, mu, eps_t, eta_n;
 };
 
-// Rigid surface: analytic sphere or quadratic B-spline SDF on a voxel grid.
+// Rigid surface: analytic sphere, quadratic B-spline SDF on a voxel grid, or
+// analytic plane.
 struct SurfaceDev {
-  int kind;                // 0 sphere, 1 SDF
+  int kind;                // 0 sphere, 1 SDF, 2 plane
   double cx, cy, cz, R;    // sphere
+  int axis;                // plane: x[axis] = pos, body on the positive side
+  double pos;
   const double* coef;      // (nx+2)(ny+2)(nz+2) prefiltered coefficients, x fastest
   int nx, ny, nz;          // grid points
   double x0, y0, z0;       // first grid point
@@ -127,8 +130,14 @@ EB_DEV double sdf_eval(const SurfaceDev& s, V3 x, V3* grad, M3* hess) {
   return v;
 }
 
+EB_DEV double axis_coord(V3 x, int a) { return a == 0 ? x.x : (a == 1 ? x.y : x.z); }
+
+// PlaneSurface (def_interactions.jl:24-27) has no gap method in the reference; the one
+// here follows the sphere's convention (utils_compute…:2-36): gap = x[axis] - pos - r,
+// gradient e_axis, Hessian zero, contact when gap <= r/4.
 EB_DEV bool incontact(const SurfaceDev& s, V3 x, double rb) {
   double gbar = rb / 4;
+  if (s.kind == 2) return axis_coord(x, s.axis) - s.pos - rb <= gbar;
   if (s.kind == 0) {  // utils_compute_interactions_beams.jl:23-36
     V3 aux = x - v3(s.cx, s.cy, s.cz);
     return norm(aux) - s.R - rb <= gbar;
@@ -141,6 +150,12 @@ EB_DEV bool incontact(const SurfaceDev& s, V3 x, double rb) {
 }
 
 EB_DEV void contact_gap(const SurfaceDev& s, V3 x, double rb, double* g, V3* dg, M3* d2g) {
+  if (s.kind == 2) {
+    *g = axis_coord(x, s.axis) - s.pos - rb;
+    *dg = v3(s.axis == 0 ? 1.0 : 0.0, s.axis == 1 ? 1.0 : 0.0, s.axis == 2 ? 1.0 : 0.0);
+    *d2g = zm3();
+    return;
+  }
   if (s.kind == 0) {  // utils_compute…:2-20
     V3 aux = x - v3(s.cx, s.cy, s.cz);
     double na = norm(aux);

@@ -108,6 +108,11 @@ extern "C" int eb_contact_eval(int64_t n, const double* in, const double* gauss6
   std::memset(&s, 0, sizeof(s));
   s.kind = (int)surf[0];
   s.cx = surf[1]; s.cy = surf[2]; s.cz = surf[3]; s.R = surf[4];
+  if (s.kind == 2) {
+    s.axis = (int)surf[1];
+    s.pos = surf[2];
+  }
+  if (s.kind < 0 || s.kind > 2 || s.axis < 0 || s.axis > 2) return EB_ERR_ARG;
   DBuf dcoef, di, dout, dfl;
   cudaError_t e;
   if (s.kind == 1) {
@@ -225,6 +230,12 @@ extern "C" int eb_contact_eval_noalloc(int64_t n, const double* d_in, const doub
   std::memset(&s, 0, sizeof(s));
   s.kind = (int)surf[0];
   s.cx = surf[1]; s.cy = surf[2]; s.cz = surf[3]; s.R = surf[4];
+  if (s.kind == 2) {
+    s.axis = (int)surf[1];
+    s.pos = surf[2];
+  }
+  if (s.kind < 0 || s.kind > 2 || s.axis < 0 || s.axis > 2)
+    return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad surface kind or plane axis");
   if (s.kind == 1) {
     const int64_t nx = (int64_t)surf[5], ny = (int64_t)surf[6], nz = (int64_t)surf[7];
     if (!d_sdf_values) return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: SDF values missing");

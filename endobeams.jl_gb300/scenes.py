@@ -24,7 +24,7 @@ import numpy as np
 
 from .api import (BeamElementSurface, Beams, BeamsConfiguration, BoundaryConditions, ConcentratedForce,
                   DiscreteSignedDistanceField, Encastre, InteractionProperties, Loads, NodesBeams,
-                  RigidInteraction, SimulationParams, SphereSurface)
+                  PlaneSurface, RigidInteraction, SimulationParams, SphereSurface)
 
 G_ACC = 9.81
 
@@ -98,11 +98,13 @@ def cantilever(n_elem: int = 20, steps: int = 2000, tol: float = 1e-8):
 
 # ------------------------------------------------------------------ configuration 1
 
-def ring_drop(n_elem: int = 64, steps: int = 5000, tol: float = 1e-8, eta_n: float = 0.0):
-    """Ring R = 10 mm in the xz plane, lowest point 2 mm above z = 0, gravity, plane SDF 64³ at 0.5 mm."""
+def ring_drop(n_elem: int = 64, steps: int = 5000, tol: float = 1e-8, eta_n: float = 0.0, surface: str = "sdf",
+              height: float = 0.002):
+    """Ring R = 10 mm in the xz plane, lowest point `height` above z = 0, gravity; the ground is the
+    plane z = 0 as an SDF 64³ at 0.5 mm (surface="sdf") or as an analytic PlaneSurface ("plane")."""
     Rr, r = 0.01, 2e-4
     ang = 2 * np.pi * np.arange(n_elem) / n_elem
-    zc = 0.002 + Rr
+    zc = height + Rr
     X = np.stack([Rr * np.cos(ang), np.zeros(n_elem), zc + Rr * np.sin(ang)], axis=1)
     conn0 = np.array([[i, (i + 1) % n_elem] for i in range(n_elem)])
     rho, E = 6500.0, 5e10
@@ -111,8 +113,11 @@ def ring_drop(n_elem: int = 64, steps: int = 5000, tol: float = 1e-8, eta_n: flo
     dofs, vals = _lumped_gravity(X, conn0, rho, r)
     conf = BeamsConfiguration(nodes, beams, Loads(_const_force(dofs, vals)), None)
     h, n = 0.5e-3, 64
-    sdf = grid_sdf(lambda x, y, z: z, (-h * (n - 1) / 2, -h * (n - 1) / 2, -0.004), h, (n, n, n))
-    inter = RigidInteraction(sdf, BeamElementSurface(conn0 + 1), InteractionProperties(1e4, 0.3, 1e-3, eta_n))
+    if surface == "plane":
+        master = PlaneSurface(0.0, "z")
+    else:
+        master = grid_sdf(lambda x, y, z: z, (-h * (n - 1) / 2, -h * (n - 1) / 2, -0.004), h, (n, n, n))
+    inter = RigidInteraction(master, BeamElementSurface(conn0 + 1), InteractionProperties(1e4, 0.3, 1e-3, eta_n))
     dt = 1e-4
     params = SimulationParams(**hht(-0.05), initial_timestep=dt, min_timestep=dt / 64, max_timestep=dt,
                               simulation_end_time=steps * dt, tolerance_residual=tol, tolerance_displacement=tol,

@@ -102,6 +102,9 @@ typedef struct {
 #define EB_SURFACE_NONE 0
 #define EB_SURFACE_SPHERE 1  /* SphereSurface (src/interactions/def_interactions.jl:30-33) */
 #define EB_SURFACE_SDF 2     /* DiscreteSignedDistanceField (def_interactions.jl:36-43,67-82) */
+#define EB_SURFACE_PLANE 3   /* PlaneSurface (def_interactions.jl:24-27); the reference declares it without a
+                                gap function: here gap = x[axis] - position - r, normal e_axis, the body on the
+                                positive side (the sphere's convention, utils_compute_interactions_beams.jl:2-36) */
 
 /* One simulation: the arrays of NodesBeams, Beams, BoundaryConditions, Loads and RigidInteraction. */
 typedef struct {
@@ -126,6 +129,8 @@ typedef struct {
   double sdf_origin[3], sdf_spacing[3];
   const double *sdf_values;                       /* nx*ny*nz, x fastest (VTK order) */
   int32_t sdf_inside;                             /* 1: use values as given, 0: negate (def_interactions.jl:71) */
+  int32_t plane_axis;                             /* PlaneSurface.axis: 0 x, 1 y, 2 z */
+  double plane_position;                          /* PlaneSurface.position */
 } eb_sim_desc;
 
 typedef struct eb_handle eb_handle;
@@ -188,7 +193,8 @@ int eb_get_forces(eb_handle *h, int32_t sim, double *Tint, double *Tk, double *T
  * in:  n x 96 packed records (layout in the implementation notes), out: n x 458
  * (strain, kinetic, Tint[12], Tk[12], K[144], M[144], C[144]; 12x12 column-major). */
 int eb_element_eval(int64_t n, const double *in, const double *gauss6, double *out);
-/* Contact: surf = [kind(0 sphere,1 sdf), cx, cy, cz, R, nx, ny, nz, x0, y0, z0, hx, hy, hz];
+/* Contact: surf = [kind(0 sphere,1 sdf,2 plane), cx, cy, cz, R, nx, ny, nz, x0, y0, z0, hx, hy, hz]
+ * (plane: [2, axis, position, ...]);
  * values = SDF grid (x fastest) when kind = 1; props = [kn, mu, eps_t, eta_n];
  * out n x 301 (energy, Tc[12], Kc[144], Cc[144]); flags[n] = 1 if any Gauss point touched. */
 int eb_contact_eval(int64_t n, const double *in, const double *gauss6, const double *props, const double *surf,

@@ -31,7 +31,9 @@ def scene_from_conf(conf, inter=None) -> O.Scene:
         m, p = inter.master, inter.properties
         sc.contact_props = (p.kn, p.mu, p.eps_t, p.eta_n)
         sc.contact_elems = np.asarray(inter.slave.contact_beams, np.int64)
-        if hasattr(m, "values"):
+        if hasattr(m, "axis_index"):
+            sc.surface = dict(kind="plane", axis=m.axis_index, position=float(m.position))
+        elif hasattr(m, "values"):
             vals = np.asarray(m.values, float)
             sc.surface = dict(kind="sdf", field=vals if m.inside else -vals, x0=m.origin, h=m.spacing)
         else:

@@ -45,9 +45,11 @@ void compute_beams(const double* in, const Gauss& g, double* out);
 
 // ---- rigid surfaces (src/interactions/*) ----
 struct Surface {
-  int kind;            // 0 = SphereSurface, 1 = DiscreteSignedDistanceField (quadratic B-spline)
+  int kind;            // 0 = SphereSurface, 1 = DiscreteSignedDistanceField (quadratic B-spline), 2 = PlaneSurface
   double center[3];    // sphere
   double radius;       // sphere
+  int axis;            // plane: 0 x, 1 y, 2 z (PlaneSurface.axis)
+  double position;     // plane: PlaneSurface.position along the axis
   const double* coef;  // SDF: prefiltered coefficients, (nx+2)*(ny+2)*(nz+2), x fastest
   int64_t nx, ny, nz;  // SDF grid points
   double x0[3];        // SDF origin (first grid point)
@@ -64,7 +66,7 @@ void compute_contact_beams(const double* in, const Gauss& g, const ContactProps&
 void regularize_gap_penalty(double gap, double rb, double* p, double* dp, double* Pi);
 void smoothstep_transition(double value, double pos, double rb, double* s, double* ds);
 
-bool incontact(const V3& x, const Surface& s, double rb);                      // utils_compute…:23-36, 67-75
+bool incontact(const V3& x, const Surface& s, double rb);                      // utils_compute…:23-36, 67-75; plane below
 void contact_gap(const V3& x, const Surface& s, double rb, double* g, V3* dg, M3* d2g);  // utils_compute…:2-20, 50-64
 
 // Quadratic B-spline SDF (Interpolations.jl 0.15.1, BSpline(Quadratic(Reflect(OnCell())))).

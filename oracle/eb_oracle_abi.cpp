@@ -11,9 +11,11 @@ using namespace orc;
 namespace {
 
 Surface make_surface(const double* s, const double* coef) {
-  // s = [kind, cx, cy, cz, R, nx, ny, nz, x0, y0, z0, hx, hy, hz]
+  // s = [kind, cx, cy, cz, R, nx, ny, nz, x0, y0, z0, hx, hy, hz]; plane (kind 2): [2, axis, position, ...]
   Surface f;
   f.kind = (int)s[0];
+  f.axis = f.kind == 2 ? (int)s[1] : 0;
+  f.position = f.kind == 2 ? s[2] : 0.0;
   f.center[0] = s[1]; f.center[1] = s[2]; f.center[2] = s[3];
   f.radius = s[4];
   f.nx = (int64_t)s[5]; f.ny = (int64_t)s[6]; f.nz = (int64_t)s[7];

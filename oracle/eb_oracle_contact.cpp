@@ -170,8 +170,13 @@ static bool isinside(const V3& p, const Surface& s) {  // utils_compute_interact
   return ok;
 }
 
+// PlaneSurface (def_interactions.jl:24-27) has no gap method in the reference.  The
+// one used here follows the sphere's convention (utils_compute…:2-36) with the body
+// on the positive side of the plane x[axis] = position: gap = x[axis] - position - r,
+// gradient e_axis, Hessian zero; contact when gap <= r/4.
 bool incontact(const V3& x, const Surface& s, double rb) {
   double gbar = rb / 4;
+  if (s.kind == 2) return x[s.axis] - s.position - rb <= gbar;
   if (s.kind == 0) {  // utils_compute_interactions_beams.jl:23-36
     V3 aux = x - v3(s.center[0], s.center[1], s.center[2]);
     double g = norm(aux) - s.radius - rb;
@@ -185,6 +190,12 @@ bool incontact(const V3& x, const Surface& s, double rb) {
 }
 
 void contact_gap(const V3& x, const Surface& s, double rb, double* g, V3* dg, M3* d2g) {
+  if (s.kind == 2) {
+    *g = x[s.axis] - s.position - rb;
+    *dg = v3(s.axis == 0 ? 1.0 : 0.0, s.axis == 1 ? 1.0 : 0.0, s.axis == 2 ? 1.0 : 0.0);
+    *d2g = zm3();
+    return;
+  }
   if (s.kind == 0) {  // utils_compute_interactions_beams.jl:2-20
     V3 aux = x - v3(s.center[0], s.center[1], s.center[2]);
     double na = norm(aux);

@@ -46,9 +46,8 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle library (make, in-tree) and return its path."""
-    if force or not os.path.exists(LIB_PATH):
-        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    """Compile the oracle library (make, in-tree; rebuilt when a source is newer) and return its path."""
+    subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []), check=True)
     return LIB_PATH
 
 
@@ -218,11 +217,13 @@ class Scene:
     force_fn: Optional[Callable[[float, int], float]] = None  # (t, 1-based dof)
     contact_props: Optional[tuple] = None  # (kn, mu, eps_t, eta_n)
     surface: Optional[dict] = None  # {"kind": "sphere", center, radius} | {"kind": "sdf", field, x0, h}
+    #                                | {"kind": "plane", axis (0..2), position}
     contact_elems: Optional[np.ndarray] = None
 
 
 def surface_arrays(surface: Optional[dict]):
-    """Packs a surface into the [kind, cx, cy, cz, R, nx, ny, nz, x0(3), h(3)] record + coefficients."""
+    """Packs a surface into the [kind, cx, cy, cz, R, nx, ny, nz, x0(3), h(3)] record + coefficients
+    (a plane as [2, axis, position, 0 ...])."""
     s = np.zeros(14)
     coef = None
     if surface is None:
@@ -231,6 +232,10 @@ def surface_arrays(surface: Optional[dict]):
         s[0] = 0
         s[1:4] = surface["center"]
         s[4] = surface["radius"]
+    elif surface["kind"] == "plane":
+        s[0] = 2
+        s[1] = surface["axis"]
+        s[2] = surface["position"]
     else:
         field = np.asarray(surface["field"], float)
         nz, ny, nx = field.shape

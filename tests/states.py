@@ -69,6 +69,29 @@ def contact_states(n, center, Rs, rb, seed=1):
     return inp
 
 
+def plane_states(n, axis, position, rb, seed=2, spread=0.2):
+    """Elements lying across the plane x[axis] = position (within ±spread in the plane),
+    tilted slightly out of it, so that most Gauss points touch."""
+    rng = np.random.default_rng(seed)
+    normal = np.zeros(3)
+    normal[axis] = 1.0
+    inp = contact_states(n, np.zeros(3), 1.0, rb, seed=seed)
+    for e in range(n):
+        p = inp[e]
+        l0 = p[72]
+        mid = rng.uniform(-spread, spread, 3)
+        mid[axis] = position + rb * rng.uniform(-0.5, 1.2)
+        t = rng.normal(size=3)
+        t[axis] = 0.0
+        t /= np.linalg.norm(t)
+        t = t + normal * rng.uniform(-0.05, 0.05)
+        t /= np.linalg.norm(t)
+        X1, X2 = mid - 0.5 * l0 * t, mid + 0.5 * l0 * t
+        p[0:3], p[3:6] = X1, X2
+        p[73:82] = O.get_Re0(X1[None], X2[None])[0]
+    return inp
+
+
 def rel_err(a, b, floor=1e-300):
     """Per-row normwise relative error ‖a-b‖/‖b‖."""
     return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), floor)

@@ -11,7 +11,7 @@ relative, so those blocks are held to 1e-10.
 import numpy as np
 import pytest
 
-from states import beam_states, contact_states, rel_err
+from states import beam_states, contact_states, plane_states, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -90,3 +90,21 @@ def test_contact_sdf_parity(eb, O):
     for name, a, b in [("E", 0, 1), ("Tc", 1, 13), ("K", 13, 157), ("C", 157, 301)]:
         err = rel_err(out[touched, a:b], ref[touched, a:b])
         assert err.max() <= 1e-10, f"{name}: {err.max():.3e}"
+
+
+@pytest.mark.parametrize("axis", [0, 2])
+def test_contact_plane_parity(eb, O, axis):
+    """Analytic PlaneSurface (x[axis] = 0.013) against the oracle's plane."""
+    rb, position = 0.01, 0.013
+    props = np.array([1e4, 0.3, 1e-3, 0.5])
+    surf = np.zeros(14)
+    surf[0], surf[1], surf[2] = 2, axis, position
+    inp = plane_states(512, axis, position, rb, seed=21 + axis)
+    ref = O.compute_contact_batch(inp, props, surf, None)
+    out, flags = eb.contact_eval(inp, props, surf)
+    touched = np.linalg.norm(ref[:, 13:157], axis=1) > 0
+    assert touched.sum() > 300
+    assert np.array_equal(flags.astype(bool), touched)
+    for name, a, b, tol in [("E", 0, 1, 1e-9), ("Tc", 1, 13, 1e-12), ("K", 13, 157, 1e-12), ("C", 157, 301, 1e-12)]:
+        err = rel_err(out[touched, a:b], ref[touched, a:b])
+        assert err.max() <= tol, f"{name}: {err.max():.3e}"

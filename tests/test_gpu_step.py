@@ -45,6 +45,19 @@ def test_ring_drop_steps(eb, O, scenes):
     assert err <= 1e-6 * 0.02, err
 
 
+def test_ring_on_analytic_plane_steps(eb, O, scenes):
+    """Ring resting on an analytic PlaneSurface from the first step (contact in
+    every step): step counts equal, positions within 1e-6 of the ring size."""
+    conf, p, inter = scenes.ring_drop(steps=60, surface="plane", height=2.2e-4)
+    p.tolerance_residual = 1e-5
+    ref, rr = _oracle_run(O, conf, p, inter)
+    res = eb.run_simulation(conf, p, inter)
+    assert res.steps[0] == rr["steps"]
+    assert list(res.ks[0]) == list(rr["ks"])
+    err = np.abs(conf.nodes.un - ref.un).max()
+    assert err <= 1e-6 * 0.02, err
+
+
 def test_batch_matches_single(eb, scenes):
     """A simulation's result does not depend on the other simulations in its batch (bitwise)."""
     p = scenes.cantilever(steps=5)[1]
