@@ -73,6 +73,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-batch and single-stent legs")
+    ap.add_argument("--output-every", type=int, default=0,
+                    help="add a VTK-output leg: write every K steps (0: off)")
+    ap.add_argument("--output-sims", type=int, default=16, help="simulations of the VTK-output leg")
+    ap.add_argument("--output-dir", default=None, help="directory of the VTK-output leg (default: a temporary one)")
     return ap.parse_args()
 
 
@@ -357,6 +361,54 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
     return out
 
 
+def output_leg(eb, wl, args):
+    """Steps/s of the first `--output-sims` simulations with VTK output every `--output-every`
+    steps (asynchronous writer, files on disk) against the same steps without output."""
+    import shutil
+    import tempfile
+    idx = list(range(min(args.output_sims, wl.count)))
+    built = [wl.build(i) for i in idx]
+    confs, inters, params = [b[0] for b in built], [b[2] for b in built], built[0][1]
+    res = {}
+    root = args.output_dir or tempfile.mkdtemp(prefix="eb_vtk_")
+    n_steps = max(args.steps, args.output_every)
+    for with_out in (False, True):
+        eng = eb.GpuSimulations(confs, params, inters)
+        drv = Driver(eng, params, [len(c.beams) for c in confs])
+        for _ in range(args.warmup):
+            drv.step()
+        drv.reset()
+        if with_out:
+            dirs = eb.api.output_dirs(root, len(idx))
+            eng.vtk_open(dirs)
+        writes, t_call = 0, 0.0
+        t0 = time.perf_counter()
+        for k in range(n_steps):
+            drv.step()
+            if with_out and (k + 1) % args.output_every == 0:
+                c0 = time.perf_counter()
+                eng.vtk_write(writes, k + 1, drv.t)
+                t_call += time.perf_counter() - c0
+                writes += 1
+        if with_out:
+            eng.vtk_flush()
+        wall = time.perf_counter() - t0
+        if with_out:
+            eng.vtk_close()
+        eng.close()
+        res["with" if with_out else "without"] = {"steps_per_s": drv.ok_steps / wall, "wall_s": wall}
+        if with_out:
+            nbytes = sum(os.path.getsize(os.path.join(dp, f)) for dp, _, fs in os.walk(root) for f in fs)
+            res["with"].update(writes=writes, files_bytes=nbytes, mean_vtk_write_call_ms=1e3 * t_call / max(writes, 1))
+    if args.output_dir is None:
+        shutil.rmtree(root, ignore_errors=True)
+    res["every"] = args.output_every
+    res["sims"] = len(idx)
+    res["steps"] = n_steps
+    res["overhead_frac"] = 1 - res["with"]["steps_per_s"] / res["without"]["steps_per_s"]
+    return res
+
+
 def gmres_bytes_per_iter(wl, idx):
     """Algorithmic bytes one GMRES iteration reads per simulation (FP32 band L and U, the
     32x32 diagonal-block inverses, the FP32 tangent and its block index), summed over idx."""
@@ -467,6 +519,8 @@ def gpu_arm(args, rank, world):
                                    "newton_iters_per_step": r["newton"] / max(r["sim_steps"], 1),
                                    "workload": single.describe(r["nodes"], r["elements"], 1)["workload"]}
         out["speedup_vs_plain_single_sim"] = value / sv
+    if args.output_every > 0:
+        out["vtk_output"] = output_leg(eb, wl, args)
     return out, wl
 
 

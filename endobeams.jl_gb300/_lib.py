@@ -101,6 +101,11 @@ SIGNATURES = {
     "eb_set_loads_all": (C.c_int, [C.c_void_p, P_d]),
     "eb_get_displacements": (C.c_int, [C.c_void_p, P_d]),
     "eb_fp64_peak": (C.c_int, [P_d]),
+    "eb_beam_output": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P_d]),
+    "eb_vtk_open": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.c_int32]),
+    "eb_vtk_write": (C.c_int, [C.c_void_p, P_i32, P_i32, P_i32, P_d]),
+    "eb_vtk_flush": (C.c_int, [C.c_void_p]),
+    "eb_vtk_close": (C.c_int, [C.c_void_p]),
     "eb_contact_eval_noalloc": (C.c_int, [C.c_int64, C.c_void_p, P_d, P_d, P_d, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
 }

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 import time
 from dataclasses import dataclass, field
 from typing import Callable, List, Optional, Sequence
@@ -456,6 +457,38 @@ class GpuSimulations:
         check(self.L.eb_get_phase_times(self.h, ptr(ms), ptr(n, C.c_int64), 1 if reset else 0), "eb_get_phase_times")
         return dict(zip(_lib.PHASES, ms)), dict(zip(_lib.PHASES, n))
 
+    # ---- output (src/IO/visualization_beams.jl)
+    def beam_output(self, s: int, points_per_beam: int = 10) -> dict:
+        """recompute_at_gausspts_beams! of simulation s's current state (visualization_beams.jl:122-162):
+        points, displacement, velocity (NP x 3), strain, stress (NP), NP = n_elem * points_per_beam."""
+        ne = len(self.confs[s].beams)
+        NP = ne * int(points_per_beam)
+        out = np.zeros(11 * NP)
+        check(self.L.eb_beam_output(self.h, int(s), int(points_per_beam), ptr(out)), "eb_beam_output")
+        return dict(points=out[:3 * NP].reshape(NP, 3), displacement=out[3 * NP:6 * NP].reshape(NP, 3),
+                    velocity=out[6 * NP:9 * NP].reshape(NP, 3), strain=out[9 * NP:10 * NP], stress=out[10 * NP:])
+
+    def vtk_open(self, dirs, points_per_beam: int = 10):
+        """Starts asynchronous VTK output: one directory per simulation (None or "" = none)."""
+        arr = (C.c_char_p * self.n)(*[(d or "").encode() for d in dirs])
+        check(self.L.eb_vtk_open(self.h, arr, int(points_per_beam)), "eb_vtk_open")
+
+    def vtk_write(self, counter, step, t, mask=None):
+        """Queues beams_<counter>.vtp and beams_nodes_<counter>.vtp of the simulations in mask
+        (write_VTK_beams, visualization_beams.jl:74-120); returns before the files are written."""
+        c, st, tt = (np.ascontiguousarray(np.broadcast_to(x, (self.n,)), dtype=dt)
+                     for x, dt in ((counter, np.int32), (step, np.int32), (t, np.float64)))
+        m = None if mask is None else i32(mask)
+        check(self.L.eb_vtk_write(self.h, ptr(m, C.c_int32) if m is not None else None, ptr(c, C.c_int32),
+                                  ptr(st, C.c_int32), ptr(tt)), "eb_vtk_write")
+
+    def vtk_flush(self):
+        check(self.L.eb_vtk_flush(self.h), "eb_vtk_flush")
+
+    def vtk_close(self):
+        """Waits for the queued files and writes each directory's simulation.pvd."""
+        check(self.L.eb_vtk_close(self.h), "eb_vtk_close")
+
     # ---- learned warm start
     def set_warm_start(self, model):
         """Installs a warm_start.WarmStartModel (None removes it)."""
@@ -525,11 +558,24 @@ class RunResult:
     krylov_iterations: List[int] = field(default_factory=list)
 
 
+def output_dirs(output_dir: str, n: int) -> List[str]:
+    """Output directory of each simulation: output_dir itself for one simulation, else
+    output_dir/sim_<index> (five digits)."""
+    if n == 1:
+        return [output_dir]
+    return [os.path.join(output_dir, f"sim_{s:05d}") for s in range(n)]
+
+
 def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Optional[int] = None,
-                    engine: Optional[GpuSimulations] = None, on_step=None) -> RunResult:
+                    engine: Optional[GpuSimulations] = None, on_step=None, points_per_beam: int = 10) -> RunResult:
     """The time loop of run_simulation! (run_simulation.jl:170-244) for many
     configurations at once: each keeps its own t, Δt and success counter, and
-    all simulations still running advance together in one batched step."""
+    all simulations still running advance together in one batched step.
+
+    With params.output_dir set, VTK files are written as the reference does
+    (run_simulation.jl:30-32, 86-90: the initial state, then after a converged
+    step once output_timestep has passed, labelled with the step's start time),
+    by the library's asynchronous writer (one directory per simulation)."""
     eng = engine or GpuSimulations(confs, params, inters)
     p = params
     S = eng.n
@@ -540,6 +586,13 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
     ks = [[] for _ in range(S)]
     newton = np.zeros(S, int)
     krylov = np.zeros(S, int)
+    out = bool(p.output_dir)
+    if out:
+        eng.vtk_open(output_dirs(p.output_dir, S), points_per_beam)
+        counter = np.zeros(S, np.int32)
+        write_t = np.zeros(S)
+        eng.vtk_write(counter, step, t)
+        counter += 1
     t0 = time.perf_counter()
     while True:
         running = (p.simulation_end_time - t > 1.0e-10)
@@ -567,6 +620,15 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
         grow = ok & (succ >= p.accelerate_after_success_it) & (k <= 8)  # :211-216
         dt[grow] = np.minimum(dt[grow] * 1.5, p.max_timestep)
         succ[grow] = 0
+        if out:
+            t1 = t + dt_used
+            due = write_t + p.output_timestep
+            tol = math.sqrt(np.finfo(float).eps) * np.maximum(np.abs(t1), np.abs(due))
+            w = ok & ((t1 > due) | (np.abs(t1 - due) <= tol))           # run_simulation.jl:86-90
+            if w.any():
+                eng.vtk_write(counter, step, t, mask=w.astype(np.int32))
+                counter[w] += 1
+                write_t[w] = t1[w]
         if ok.any():
             eng.commit(ok.astype(np.int32))              # update_converged!, :232
         for s in np.nonzero(ok)[0]:
@@ -575,6 +637,8 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
         step[ok] += 1
         if on_step is not None:
             on_step(eng, ok, k)
+    if out:
+        eng.vtk_close()
     wall = time.perf_counter() - t0
     eng.sync_nodes()
     return RunResult(steps=list(step - 1), ks=ks, t=list(t), wall_s=wall, newton_iterations=list(newton),

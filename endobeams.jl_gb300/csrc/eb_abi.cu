@@ -15,6 +15,7 @@
 #include "../../include/endobeams_gb300.h"
 #include "eb_gmres.cuh"
 #include "eb_internal.cuh"
+#include "eb_output.cuh"
 #include "eb_warm.cuh"
 
 using namespace eb;
@@ -340,6 +341,9 @@ struct eb_handle {
   int64_t* d_fix_dof = nullptr;
   double* d_vals = nullptr;                // scratch for set_loads / set_imposed
   double* d_u3 = nullptr;                  // n_nodes x 3 scratch for eb_get_displacements (first use)
+  // output pipeline
+  double* d_E = nullptr;                   // per element
+  VtkWriter* vtk = nullptr;
   // per-sim device arrays
   int* d_mask = nullptr;
   int* d_active = nullptr;
@@ -653,7 +657,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   std::vector<double> R(9 * NN), dR(9 * NN, 0.0);
   std::vector<int> node_sim(NN);
   std::vector<int> ea(NE), ebv(NE), elem_sim(NE);
-  std::vector<double> l0(NE), Re0(9 * NE), Kbar(7 * NE), Jr(3 * NE), Ar(NE), damp(NE), radius(NE);
+  std::vector<double> l0(NE), Re0(9 * NE), Kbar(7 * NE), Jr(3 * NE), Ar(NE), damp(NE), radius(NE), Ev(NE);
   std::vector<uint8_t> is_contact(NE, 0);
   std::vector<uint8_t> fixed(ND, 0);
   std::vector<double> fext(ND, 0.0);
@@ -707,6 +711,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
       Ar[ge] = rho * A;
       damp[ge] = S.damping[e];
       radius[ge] = r;
+      Ev[ge] = E;
     }
     // contact
     if (S.surface != EB_SURFACE_NONE) {
@@ -924,6 +929,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   CK(A.upload(&p_l0, l0)); CK(A.upload(&p_Re0, Re0)); CK(A.upload(&p_Kb, Kbar)); CK(A.upload(&p_Jr, Jr));
   CK(A.upload(&p_Ar, Ar)); CK(A.upload(&p_dm, damp)); CK(A.upload(&p_rd, radius));
   d.l0 = p_l0; d.Re0 = p_Re0; d.Kbar = p_Kb; d.Jr = p_Jr; d.Ar = p_Ar; d.damp = p_dm; d.radius = p_rd;
+  CK(A.upload(&h->d_E, Ev));  // Young's modulus per element, for the stress output
   uint8_t* p_ic;
   CK(A.upload(&p_ic, is_contact));
   d.is_contact = p_ic;
@@ -1098,6 +1104,11 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
 
 int eb_destroy(eb_handle* h) {
   if (!h) return EB_OK;
+  if (h->vtk) {
+    std::string err;
+    vtk_close(h->vtk, err);
+    h->vtk = nullptr;
+  }
   if (h->stream) {
     cudaStreamSynchronize(h->stream);
     cudaStreamDestroy(h->stream);
@@ -1194,6 +1205,64 @@ int eb_get_displacements(eb_handle* h, double* u) {
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(u, h->d_u3, sizeof(double) * 3 * NN, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  return EB_OK;
+}
+
+int eb_beam_output(eb_handle* h, int32_t sim, int32_t points_per_beam, double* out) {
+  if (!h || !out || sim < 0 || sim >= h->n_sims) return fail(EB_ERR_ARG, "eb_beam_output: bad arguments");
+  if (points_per_beam < 2) return fail(EB_ERR_ARG, "eb_beam_output: points_per_beam must be at least 2");
+  const int64_t e0 = h->elem_off[sim], ne = h->elem_off[sim + 1] - e0;
+  const size_t n = (size_t)beam_output_doubles(ne, points_per_beam);
+  double* dbuf = nullptr;
+  CK(cudaMalloc(&dbuf, sizeof(double) * n));
+  launch_beam_output(h->d, h->d_E, e0, ne, points_per_beam, dbuf, h->stream);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dbuf, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(dbuf);
+  CK(e);
+  return EB_OK;
+}
+
+int eb_vtk_open(eb_handle* h, const char* const* dirs, int32_t points_per_beam) {
+  if (!h || !dirs) return fail(EB_ERR_ARG, "eb_vtk_open: bad arguments");
+  if (h->vtk) return fail(EB_ERR_STATE, "eb_vtk_open: output already open (eb_vtk_close first)");
+  std::vector<VtkSim> sims(h->n_sims);
+  std::vector<std::string> ds(h->n_sims);
+  for (int s = 0; s < h->n_sims; ++s) {
+    sims[s] = VtkSim{h->elem_off[s], h->elem_off[s + 1] - h->elem_off[s], h->node_off[s],
+                     h->node_off[s + 1] - h->node_off[s]};
+    ds[s] = dirs[s] ? dirs[s] : "";
+  }
+  std::string err;
+  h->vtk = vtk_open(h->d, h->d_E, h->stream, sims, ds, points_per_beam, err);
+  if (!h->vtk) return fail(EB_ERR_ARG, "eb_vtk_open: %s", err.c_str());
+  return EB_OK;
+}
+
+int eb_vtk_write(eb_handle* h, const int32_t* mask, const int32_t* counter, const int32_t* step, const double* t) {
+  if (!h || !counter || !step || !t) return fail(EB_ERR_ARG, "eb_vtk_write: bad arguments");
+  if (!h->vtk) return fail(EB_ERR_STATE, "eb_vtk_write: output not open (eb_vtk_open)");
+  std::string err;
+  if (vtk_write(h->vtk, mask, counter, step, t, err)) return fail(EB_ERR_CUDA, "%s", err.c_str());
+  return EB_OK;
+}
+
+int eb_vtk_flush(eb_handle* h) {
+  if (!h) return fail(EB_ERR_ARG, "eb_vtk_flush: null handle");
+  if (!h->vtk) return EB_OK;
+  std::string err;
+  if (vtk_flush(h->vtk, err)) return fail(EB_ERR_IO, "eb_vtk_flush: %s", err.c_str());
+  return EB_OK;
+}
+
+int eb_vtk_close(eb_handle* h) {
+  if (!h) return fail(EB_ERR_ARG, "eb_vtk_close: null handle");
+  if (!h->vtk) return EB_OK;
+  std::string err;
+  const int rc = vtk_close(h->vtk, err);
+  h->vtk = nullptr;
+  if (rc) return fail(EB_ERR_IO, "eb_vtk_close: %s", err.c_str());
   return EB_OK;
 }
 

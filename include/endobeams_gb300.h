@@ -46,6 +46,7 @@ extern "C" {
 #define EB_ERR_CUDA (-2)
 #define EB_ERR_NOMEM (-3)
 #define EB_ERR_STATE (-4)
+#define EB_ERR_IO (-5)
 
 /* per-simulation status written by eb_step */
 #define EB_SIM_OK 0
@@ -188,6 +189,27 @@ int eb_get_stats(eb_handle *h, eb_sim_stats *stats /* n_sims */);
 int eb_get_memory(eb_handle *h, int64_t *device_bytes, int32_t *band_sims);
 /* Assembled global vectors of one simulation at n+1 (6 n_nodes each; NULL to skip). */
 int eb_get_forces(eb_handle *h, int32_t sim, double *Tint, double *Tk, double *Tc);
+
+/* ---- output (src/IO/visualization_beams.jl) ----
+ * recompute_at_gausspts_beams! (visualization_beams.jl:122-162) of one simulation's current
+ * state: points_per_beam (>= 2) points per element at z = range(-1, 1, length = points_per_beam),
+ * point k = points_per_beam * e + i.  out (host) receives 11 * n_elem * points_per_beam doubles:
+ * [x (3 per point) | displacement (3) | velocity (3) | strain (1 per point) | stress (1)]. */
+#define EB_OUT_FIELDS 11
+int eb_beam_output(eb_handle *h, int32_t sim, int32_t points_per_beam, double *out);
+/* Asynchronous VTK output, replacing VTKDataBeams + write_VTK_beams (visualization_beams.jl:28-120).
+ * dirs[n_sims]: output directory per simulation (NULL or "" = no output), created if missing;
+ * existing files are overwritten, other files are left alone.  Each eb_vtk_write queues, for every
+ * simulation with mask[s] != 0 (NULL: all) and a directory, beams_<counter[s]>.vtp (interpolated
+ * beams: Stress, Strain, Displacement, Velocity; field data time = t[s], step = step[s]) and
+ * beams_nodes_<counter[s]>.vtp (nodes: Displacement, In Contact, Contact Force, Contact Distance)
+ * of the state at this point of the handle's stream, and returns; a writer thread writes them
+ * (VTK XML PolyData, appended raw data).  eb_vtk_flush waits for the queued files and reports the
+ * first write error (EB_ERR_IO); eb_vtk_close also writes each directory's simulation.pvd. */
+int eb_vtk_open(eb_handle *h, const char *const *dirs, int32_t points_per_beam);
+int eb_vtk_write(eb_handle *h, const int32_t *mask, const int32_t *counter, const int32_t *step, const double *t);
+int eb_vtk_flush(eb_handle *h);
+int eb_vtk_close(eb_handle *h);
 
 /* Testing entry points: evaluate single elements on the device.
  * in:  n x 96 packed records (layout in the implementation notes), out: n x 458

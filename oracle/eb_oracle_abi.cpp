@@ -163,6 +163,47 @@ void orc_assemble(int64_t n_nodes, int64_t n_elem, const double* X0, const doubl
   energies[2] = ec;
 }
 
+// recompute_at_gausspts_beams! (src/IO/visualization_beams.jl:122-162): per element,
+// `pts` points at z = range(-1, 1, length = pts) along the beam, interpolated with the
+// linear (axial) and cubic (bending, in the local frame) shape functions.  Output
+// block of NP = n_elem * pts points: [x (3 NP) | displacement (3 NP) | velocity (3 NP) |
+// strain (NP) | stress (NP)], point k = pts * e + i.
+void orc_beam_output(int64_t n_elem, const double* X0, const double* u, const double* ud, const double* R,
+                     const int64_t* conn, const double* l0v, const double* Re0v, const double* E, int32_t pts,
+                     double* out) {
+  const int64_t NP = n_elem * pts;
+  double *ox = out, *od = out + 3 * NP, *ov = out + 6 * NP, *oe = out + 9 * NP, *os = out + 10 * NP;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int64_t a = conn[2 * e], b = conn[2 * e + 1];
+    V3 X1 = v3(X0[3 * a], X0[3 * a + 1], X0[3 * a + 2]), X2 = v3(X0[3 * b], X0[3 * b + 1], X0[3 * b + 2]);
+    V3 u1 = v3(u[3 * a], u[3 * a + 1], u[3 * a + 2]), u2 = v3(u[3 * b], u[3 * b + 1], u[3 * b + 2]);
+    V3 v1 = v3(ud[3 * a], ud[3 * a + 1], ud[3 * a + 2]), v2 = v3(ud[3 * b], ud[3 * b + 1], ud[3 * b + 2]);
+    M3 R1, R2, Re0;
+    for (int k = 0; k < 9; ++k) { R1.a[k] = R[9 * a + k]; R2.a[k] = R[9 * b + k]; Re0.a[k] = Re0v[9 * e + k]; }
+    const double l0 = l0v[e];
+    V3 x1 = X1 + u1, x2 = X2 + u2;
+    const double ln = norm(x2 - x1);
+    LocalFrame f = local_Re_and_aux(x1, x2, R1, R2, col(Re0, 1), ln);
+    V3 T1 = toangle((tr(f.Re) * R1) * Re0);
+    V3 T2 = toangle((tr(f.Re) * R2) * Re0);
+    for (int i = 0; i < pts; ++i) {
+      const int64_t k = (int64_t)pts * e + i;
+      const double z = (2.0 * i - (pts - 1)) / (double)(pts - 1);
+      const double xi = l0 * (z + 1) / 2;
+      const double N1 = 1 - xi / l0, N2 = 1 - N1;
+      const double N3 = xi * ((1 - xi / l0) * (1 - xi / l0));
+      const double N4 = -(1 - xi / l0) * ((xi * xi) / l0);
+      V3 ut = v3(0.0, N3 * T1[2] + N4 * T2[2], -N3 * T1[1] - N4 * T2[1]);
+      V3 xg = (N1 * x1 + N2 * x2) + f.Re * ut;
+      V3 dg = N1 * u1 + N2 * u2;
+      V3 vg = N1 * v1 + N2 * v2;
+      for (int c = 0; c < 3; ++c) { ox[3 * k + c] = xg[c]; od[3 * k + c] = dg[c]; ov[3 * k + c] = vg[c]; }
+      oe[k] = 1 - ln / l0;
+      os[k] = E[e] * (1 - ln / l0);
+    }
+  }
+}
+
 // compute_local_predictor! (utils_solver.jl:197-217).  D, Dd, Ddd are the
 // global 6n vectors; node arrays are updated in place.
 void orc_local_predictor(int64_t n, const double* D, const double* Dd, const double* Ddd, double* u, double* ud,

@@ -65,6 +65,7 @@ def lib():
         L.orc_sdf_eval_batch.argtypes = [P, P, I, P, D, P]
         L.orc_assemble.argtypes = [I, I] + [P] * 8 + [P] * 8 + [P, P, I, P, P, P, P, P, P, P, I, P, P, D, P, P]
         L.orc_local_predictor.argtypes = [I] + [P] * 14 + [D, D, D]
+        L.orc_beam_output.argtypes = [I] + [P] * 8 + [ctypes.c_int32, P]
         L.orc_local_corrector.argtypes = [I] + [P] * 14 + [D, D, D]
         _lib = L
     return _lib
@@ -264,6 +265,7 @@ class OracleModel:
         bc = lambda x: np.broadcast_to(np.asarray(x, float), (ne,)).copy()
         self.radius = bc(sc.radius)
         self.damping = bc(sc.damping)
+        self.E = _c(bc(sc.E))
         self.Kbar, self.Jr, self.Ar = beam_constants(bc(sc.E), bc(sc.nu), bc(sc.rho), self.radius, self.l0)
         self.Kbar, self.Jr, self.Ar = _c(self.Kbar), _c(self.Jr), _c(self.Ar)
         self.Re0 = _c(sc.Re0) if sc.Re0 is not None else get_Re0(self.X0[self.conn[:, 0]], self.X0[self.conn[:, 1]])
@@ -318,6 +320,23 @@ class OracleModel:
         for k in ("K", "C", "M"):
             self.m_n[k][:] = self.m_1[k]
         self.last_lin_err = 0.0
+
+    # ---- output (visualization_beams.jl:122-175)
+    def beam_output(self, pts: int = 10) -> dict:
+        """recompute_at_gausspts_beams! of the current state: per element `pts` points;
+        returns points, displacement, velocity (NP x 3), strain, stress (NP)."""
+        NP = self.ne * pts
+        out = np.zeros(11 * NP)
+        lib().orc_beam_output(self.ne, _p(self.X0), _p(self.u), _p(self.ud), _p(self.R), _p(self.conn),
+                              _p(self.l0), _p(self.Re0), _p(self.E), int(pts), _p(out))
+        return dict(points=out[:3 * NP].reshape(NP, 3), displacement=out[3 * NP:6 * NP].reshape(NP, 3),
+                    velocity=out[6 * NP:9 * NP].reshape(NP, 3), strain=out[9 * NP:10 * NP],
+                    stress=out[10 * NP:])
+
+    def node_output(self) -> dict:
+        """recompute_at_nodes_beams! (visualization_beams.jl:165-175): positions and displacements;
+        the reference never updates the nodes' contact fields, so they stay zero."""
+        return dict(points=self.X0 + self.u, displacement=self.u.copy())
 
     # ---- node state commits (utils_solver.jl:252-305)
     def commit_nodes(self):
