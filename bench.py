@@ -369,6 +369,7 @@ def output_leg(eb, wl, args):
     idx = list(range(min(args.output_sims, wl.count)))
     built = [wl.build(i) for i in idx]
     confs, inters, params = [b[0] for b in built], [b[2] for b in built], built[0][1]
+    params.warm_start = "off"
     res = {}
     root = args.output_dir or tempfile.mkdtemp(prefix="eb_vtk_")
     n_steps = max(args.steps, args.output_every)

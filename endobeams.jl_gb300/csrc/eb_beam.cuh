@@ -44,6 +44,24 @@ EB_DEV void put_blockT(double* m, int bi, int bj, const M3& b) {
     for (int i = 0; i < 3; ++i) m[(3 * bi + i) + 12 * (3 * bj + j)] = b(j, i);
 }
 EB_DEV void put_vec(double* v, int bi, V3 x) { v[3 * bi] = x.x; v[3 * bi + 1] = x.y; v[3 * bi + 2] = x.z; }
+EB_DEV M3 get_block(const double* m, int bi, int bj) {
+  M3 b;
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) b(i, j) = m[(3 * bi + i) + 12 * (3 * bj + j)];
+  return b;
+}
+// block (bi, bj) of a 12x12 column-major matrix += s q (fused multiply-add per entry)
+EB_DEV void acc_block(double* m, int bi, int bj, double s, const M3& q) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      double& x = m[(3 * bi + i) + 12 * (3 * bj + j)];
+      x = fma(s, q(i, j), x);
+    }
+}
 
 // Element frame and auxiliaries of local_Rₑ_and_aux (utils_beams.jl:35-87).
 struct Frame {

@@ -221,11 +221,15 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
   *any_contact = touched;
   if (!touched) return;
 
+  // Kᶜ and Cᶜ are summed over the Gauss points in the element's staging blocks (global
+  // memory, this thread's own 2 x 144 doubles) rather than in 288 accumulator registers,
+  // which spilled; the sums, their order and the final scaling are the same.
   double energy = 0.0;
   V3 Tc[4] = {zv3(), zv3(), zv3(), zv3()};
-  M3 Kc[16], Cc[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) { Kc[k] = zm3(); Cc[k] = zm3(); }
+  for (int k = 0; k < 144; ++k) {
+    out.K[k] = 0.0;
+    out.C[k] = 0.0;
+  }
 
 #pragma unroll 1
   for (int ig = 0; ig < 3; ++ig) {
@@ -280,23 +284,11 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
 #pragma unroll
     for (int i = 0; i < 4; ++i) Tc[i] += wg * mulTv(RHR[i], fc);
 
-    // t₁ + t₃ (:128-155, :186-209): Rₑ[-S(H₁ⁱᵀ𝓕ᶜ) + H₁ⁱᵀS(𝓕ᶜ)] Gʲ Rₑᵀ, j = 1,2,4 (t^{i3} = -t^{i1})
+    // t₂ factors (:157-184)
     M3 SFc = skew(Fc);
-    M3 t13[4][3];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      M3 Li = Re * (mulTN(H1[i], SFc) - skew(mulTv(H1[i], Fc)));
-      t13[i][0] = Li * G1ReT;
-      t13[i][1] = Li * G2ReT;
-      t13[i][2] = Li * G4ReT;
-    }
-    // t₂ (:157-184)
     M3 A1Fr = rows(0, 0, 0, Fc.y * v1.x, Fc.y * v1.y, Fc.y * v1.z, Fc.z * v1.x, Fc.z * v1.y, Fc.z * v1.z);
     M3 SFP1 = muld(SFc, v3(0.0, N7l, N7l)) * ReT, SFP2 = (SFc * P1P2) * ReT, SFP4 = (SFc * P1P4) * ReT;
     M3 ReG1 = mulNT(Re, full(G1)), ReG2 = mulNT(Re, full(G2)), ReG4 = mulNT(Re, full(G4));
-    M3 t2_11 = N7l2 * (Re * A1Fr) - ReG1 * SFP1, t2_12 = -(ReG1 * SFP2), t2_14 = -(ReG1 * SFP4);
-    M3 t2_21 = -(ReG2 * SFP1), t2_22 = -(ReG2 * SFP2), t2_24 = -(ReG2 * SFP4);
-    M3 t2_41 = -(ReG4 * SFP1), t2_42 = -(ReG4 * SFP2), t2_44 = -(ReG4 * SFP4);
 
     // ∂u̇₀/∂d (:211-238)
     M3 aux = dot(dg, ud0) * d2g + outer(dg, d2g * ud0);
@@ -324,20 +316,28 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
       Kfc[j] = auxK * RHR[j] - eta_n * dun_d + (aux1 * RHR[j] + aux2 * dut_d);
       Cfc[j] = ((-eta_n) * nn) * RHR[j] + aux2 * dut_v;
     }
-    // accumulate (:332-370)
+    // accumulate (:332-370), one row block at a time:
+    //   t₁ + t₃ (:128-155, :186-209): Rₑ[-S(H₁ⁱᵀ𝓕ᶜ) + H₁ⁱᵀS(𝓕ᶜ)] Gʲ Rₑᵀ, j = 1,2,4 (t^{i3} = -t^{i1});
+    //   t₂ row i from ReGᵢ and SFPⱼ (row 3 is minus row 1)
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
+      M3 Li = Re * (mulTN(H1[i], SFc) - skew(mulTv(H1[i], Fc)));
+      const M3 t13_1 = Li * G1ReT, t13_2 = Li * G2ReT, t13_4 = Li * G4ReT;
+      const M3& ReGi = (i == 1) ? ReG2 : (i == 3) ? ReG4 : ReG1;
+      M3 t2_1 = (i == 0 || i == 2) ? N7l2 * (Re * A1Fr) - ReG1 * SFP1 : -(ReGi * SFP1);
+      M3 t2_2 = -(ReGi * SFP2), t2_4 = -(ReGi * SFP4);
+      if (i == 2) {
+        t2_1 = -t2_1;
+        t2_2 = -t2_2;
+        t2_4 = -t2_4;
+      }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         M3 t4 = mulTN(RHR[i], Kfc[j]);
-        M3 t13v = (j == 0) ? t13[i][0] : (j == 1) ? t13[i][1] : (j == 2) ? -t13[i][0] : t13[i][2];
-        M3 t2v;
-        if (i == 0) t2v = (j == 0) ? t2_11 : (j == 1) ? t2_12 : (j == 2) ? -t2_11 : t2_14;
-        else if (i == 1) t2v = (j == 0) ? t2_21 : (j == 1) ? t2_22 : (j == 2) ? -t2_21 : t2_24;
-        else if (i == 2) t2v = (j == 0) ? -t2_11 : (j == 1) ? -t2_12 : (j == 2) ? t2_11 : -t2_14;
-        else t2v = (j == 0) ? t2_41 : (j == 1) ? t2_42 : (j == 2) ? -t2_41 : t2_44;
-        axpy(Kc[4 * i + j], wg, (t13v + t2v) + t4);
-        axpy(Cc[4 * i + j], wg, mulTN(RHR[i], Cfc[j]));
+        M3 t13v = (j == 0) ? t13_1 : (j == 1) ? t13_2 : (j == 2) ? -t13_1 : t13_4;
+        M3 t2v = (j == 0) ? t2_1 : (j == 1) ? t2_2 : (j == 2) ? -t2_1 : t2_4;
+        acc_block(out.K, i, j, wg, (t13v + t2v) + t4);
+        acc_block(out.C, i, j, wg, mulTN(RHR[i], Cfc[j]));
       }
     }
   }
@@ -351,8 +351,8 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      put_block(out.K, i, j, l02 * Kc[4 * i + j]);
-      M3 c = l02 * Cc[4 * i + j];
+      put_block(out.K, i, j, l02 * get_block(out.K, i, j));
+      M3 c = l02 * get_block(out.C, i, j);
       if (i == 1) c = c * TaT;
       if (i == 3) c = c * TbT;
       put_block(out.C, i, j, c);

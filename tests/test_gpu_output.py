@@ -22,8 +22,10 @@ def _gpu_state_into_oracle(O, eng, conf, inter, p):
 
 @pytest.mark.parametrize("pts", [2, 10])
 def test_beam_output_matches_oracle(eb, O, scenes, pts):
-    """Ring on the analytic plane after 20 steps (bent, moving, in contact): every
-    output field within 1e-12 (normwise relative) of the oracle on the same state."""
+    """Ring on the analytic plane after 20 steps (bent, moving, in contact): positions,
+    displacements and velocities within 1e-12 (normwise relative) of the oracle on the
+    same state; strain = 1 - l/l0 is a difference of O(1) numbers (the ring's strain is
+    ~1e-8), so it is held to 1e-14 absolute and the stress to 1e-14 E."""
     conf, p, inter = scenes.ring_drop(steps=20, surface="plane", height=2.2e-4)
     p.tolerance_residual = 1e-5
     eng = eb.GpuSimulations([conf], p, [inter])
@@ -32,9 +34,11 @@ def test_beam_output_matches_oracle(eb, O, scenes, pts):
     ref = O.OracleModel.beam_output(m, pts)
     out = eng.beam_output(0, pts)
     eng.close()
-    for k in ("points", "displacement", "velocity", "strain", "stress"):
+    for k in ("points", "displacement", "velocity"):
         err = np.linalg.norm(out[k] - ref[k]) / np.linalg.norm(ref[k])
         assert err <= 1e-12, f"{k}: {err:.3e}"
+    assert np.abs(out["strain"] - ref["strain"]).max() <= 1e-14
+    assert np.abs(out["stress"] - ref["stress"]).max() <= 1e-14 * m.E.max()
 
 
 def test_vtk_files_follow_the_reference_schedule(eb, scenes, tmp_path):
@@ -42,6 +46,7 @@ def test_vtk_files_follow_the_reference_schedule(eb, scenes, tmp_path):
     simulation.pvd listing both per write; the last file holds exactly the final
     state's reinterpolation, labelled with the last step's start time and step number."""
     conf, p, inter = scenes.cantilever(steps=12)
+    p.tolerance_residual = 1e-5
     p.output_dir = str(tmp_path / "out")
     p.output_timestep = p.initial_timestep / 2
     eng = eb.GpuSimulations([conf], p, [inter])
@@ -83,6 +88,7 @@ def test_vtk_batch_directories_and_output_interval(eb, scenes, tmp_path):
     confs, inters = [], []
     for _ in range(2):
         c, p, it = scenes.cantilever(steps=9)
+        p.tolerance_residual = 1e-5
         confs.append(c)
         inters.append(it)
     p.output_dir = str(tmp_path / "batch")
