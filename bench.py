@@ -325,6 +325,7 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
     drv = Driver(eng, params, [len(c.beams) for c in confs])
     for _ in range(args.warmup):
         drv.step()
+    launch_shapes = eng.autotune()
     eng.phase_times(reset=True)
     drv.reset()
     barrier(world)
@@ -337,7 +338,8 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
            "ws_used": drv.ws_used, "ws_steps": drv.ws_steps, "phase_ms": phase_ms, "launches": launches,
            "elem_evals": drv.elem_evals,
            "nodes": sum(len(c.nodes) for c in confs), "elements": sum(len(c.beams) for c in confs),
-           "sims": len(idx), "device_bytes": mem, "band_sims": band_sims, "e2e": None}
+           "sims": len(idx), "device_bytes": mem, "band_sims": band_sims, "e2e": None,
+           "launch_shapes": launch_shapes}
     if e2e and not args.no_e2e:
         total_nodes = out["nodes"]
         ubuf = np.zeros((total_nodes, 3))
@@ -496,7 +498,8 @@ def gpu_arm(args, rank, world):
         "vs_baseline": None, "dtype": "f64" if wl.precision == "fp64" else "f64+f32-krylov", "data": "synthetic",
         "config": dict(wl.describe(tot["nodes"], tot["elements"], len(groups)),
                        l2="state, band and staging arrays exceed L2 (129 MB) each step", device=gname,
-                       device_bytes_per_group_max=int(tot["device_bytes_max"]), band_preconditioned_sims=tot["band_sims"]),
+                       device_bytes_per_group_max=int(tot["device_bytes_max"]), band_preconditioned_sims=tot["band_sims"],
+                       launch_shapes_first_group=tot["launch_shapes"]),
         "newton_iters_per_step": tot["newton"] / max(tot["sim_steps"], 1),
         "krylov_iters_per_newton": tot["krylov"] / max(tot["newton"], 1),
         "phase_ms": {k: round(v, 3) for k, v in phase_ms.items()}, "dominant_phase": dom,

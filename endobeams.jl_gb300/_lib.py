@@ -102,6 +102,8 @@ SIGNATURES = {
     "eb_get_displacements": (C.c_int, [C.c_void_p, P_d]),
     "eb_fp64_peak": (C.c_int, [P_d]),
     "eb_beam_output": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P_d]),
+    "eb_autotune": (C.c_int, [C.c_void_p, P_i32]),
+    "eb_set_launch_shapes": (C.c_int, [C.c_void_p, P_i32]),
     "eb_vtk_open": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.c_int32]),
     "eb_vtk_write": (C.c_int, [C.c_void_p, P_i32, P_i32, P_i32, P_d]),
     "eb_vtk_flush": (C.c_int, [C.c_void_p]),

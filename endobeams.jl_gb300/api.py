@@ -277,6 +277,7 @@ class SimulationParams:
                                      # 2: test of the bounded wait (the first block's wait runs out)
     warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start)
     use_graph: bool = True           # replay each Newton iteration from a CUDA graph
+    autotune: bool = True            # run_simulations: pick kernel block sizes after the first step
 
     def to_c(self) -> _lib.EbParams:
         p = _lib.default_params()
@@ -457,6 +458,17 @@ class GpuSimulations:
         check(self.L.eb_get_phase_times(self.h, ptr(ms), ptr(n, C.c_int64), 1 if reset else 0), "eb_get_phase_times")
         return dict(zip(_lib.PHASES, ms)), dict(zip(_lib.PHASES, n))
 
+    def autotune(self) -> dict:
+        """Picks the fastest block sizes of the element, contact and assembly kernels on the current
+        state (eb_autotune); results do not depend on the choice.  Call between steps."""
+        ch = np.zeros(4, np.int32)
+        check(self.L.eb_autotune(self.h, ptr(ch, C.c_int32)), "eb_autotune")
+        return dict(zip(("beam", "contact", "assembly_matrix", "assembly_vector"), (int(x) for x in ch)))
+
+    def set_launch_shapes(self, beam: int, contact: int, assembly_matrix: int, assembly_vector: int):
+        sh = np.array([beam, contact, assembly_matrix, assembly_vector], np.int32)
+        check(self.L.eb_set_launch_shapes(self.h, ptr(sh, C.c_int32)), "eb_set_launch_shapes")
+
     # ---- output (src/IO/visualization_beams.jl)
     def beam_output(self, s: int, points_per_beam: int = 10) -> dict:
         """recompute_at_gausspts_beams! of simulation s's current state (visualization_beams.jl:122-162):
@@ -586,6 +598,7 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
     ks = [[] for _ in range(S)]
     newton = np.zeros(S, int)
     krylov = np.zeros(S, int)
+    tuned = False
     out = bool(p.output_dir)
     if out:
         eng.vtk_open(output_dirs(p.output_dir, S), points_per_beam)
@@ -637,6 +650,9 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
         step[ok] += 1
         if on_step is not None:
             on_step(eng, ok, k)
+        if p.autotune and not tuned and ok.any():
+            eng.autotune()  # between steps: results do not depend on the block sizes it picks
+            tuned = True
     if out:
         eng.vtk_close()
     wall = time.perf_counter() - t0

@@ -317,6 +317,7 @@ struct IterGraph {
 };
 
 struct eb_handle {
+  bool mid_step = false;  // eb_step ran and neither eb_commit nor eb_rollback followed yet
   PhaseTimer timer;
   WsHost ws;
   // pinned host mirrors used by the captured iterations, and the graphs
@@ -845,6 +846,10 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   d.n_elem = NE;
   d.nnzb = NB;
   d.n_dof = ND;
+  d.beam_threads = kThreads;
+  d.contact_threads = kThreads;
+  d.gmat_threads = 256;
+  d.gvec_threads = 256;
   int64_t *p_node_off, *p_blk_off;
   CK(A.upload(&p_node_off, h->node_off));
   CK(A.upload(&p_blk_off, h->blk_off));
@@ -1208,6 +1213,85 @@ int eb_get_displacements(eb_handle* h, double* u) {
   return EB_OK;
 }
 
+// Launch-shape autotuner: times the element, contact and assembly kernels on the
+// current state at each candidate block size and keeps the fastest.  Every
+// candidate computes each output with the same operations in the same order (one
+// thread per element / block entry / DOF), so the choice changes no result.  The
+// kernels overwrite only the n+1 staging and assembly arrays, which every step
+// recomputes before reading them; hence the call must come between steps.
+int eb_autotune(eb_handle* h, int32_t* chosen) {
+  if (!h) return fail(EB_ERR_ARG, "eb_autotune: null handle");
+  if (h->mid_step) return fail(EB_ERR_STATE, "eb_autotune: call it between steps (after eb_commit or eb_rollback)");
+  Dev& d = h->d;
+  cudaStream_t st = h->stream;
+  const int S = h->n_sims;
+  std::vector<int> ones(S, 1);
+  CK(cudaMemcpyAsync(h->d_active, ones.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  cudaError_t err = cudaEventCreate(&e1);
+  if (err != cudaSuccess) {
+    cudaEventDestroy(e0);
+    CK(err);
+  }
+  const double alpha = h->P.alpha;
+  auto time_it = [&](int* knob, const int* cand, int nc, auto&& launch) -> cudaError_t {
+    float best = INFINITY;
+    int pick = *knob;
+    for (int c = 0; c < nc; ++c) {
+      *knob = cand[c];
+      launch();
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < 5; ++r) launch();
+      cudaEventRecord(e1, st);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        pick = cand[c];
+      }
+    }
+    *knob = pick;
+    return cudaSuccess;
+  };
+  static const int kElem[3] = {64, 128, 256}, kGather[3] = {128, 256, 512};
+  err = time_it(&d.beam_threads, kElem, 3, [&] { launch_beam(d, h->gauss, st); });
+  if (err == cudaSuccess && h->any_contact)
+    err = time_it(&d.contact_threads, kElem, 3, [&] { launch_contact(d, h->gauss, st); });
+  if (err == cudaSuccess)
+    err = time_it(&d.gmat_threads, kGather, 3, [&] { launch_gather(d, alpha, h->any_contact, st); });
+  if (err == cudaSuccess)
+    err = time_it(&d.gvec_threads, kGather, 3, [&] { launch_gather(d, alpha, h->any_contact, st); });
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(err);
+  h->graph_gen += 1;  // captured iterations hold the old launch shapes
+  if (chosen) {
+    chosen[0] = d.beam_threads;
+    chosen[1] = d.contact_threads;
+    chosen[2] = d.gmat_threads;
+    chosen[3] = d.gvec_threads;
+  }
+  return EB_OK;
+}
+
+int eb_set_launch_shapes(eb_handle* h, const int32_t* shapes) {
+  if (!h || !shapes) return fail(EB_ERR_ARG, "eb_set_launch_shapes: bad arguments");
+  for (int k = 0; k < 4; ++k) {
+    const int v = shapes[k], hi = k < 2 ? kMaxElemThreads : 1024;
+    if (v < 32 || v > hi || v % 32) return fail(EB_ERR_ARG, "eb_set_launch_shapes: shape %d = %d (multiples of 32 up to %d)", k, v, hi);
+  }
+  h->d.beam_threads = shapes[0];
+  h->d.contact_threads = shapes[1];
+  h->d.gmat_threads = shapes[2];
+  h->d.gvec_threads = shapes[3];
+  h->graph_gen += 1;
+  return EB_OK;
+}
+
 int eb_beam_output(eb_handle* h, int32_t sim, int32_t points_per_beam, double* out) {
   if (!h || !out || sim < 0 || sim >= h->n_sims) return fail(EB_ERR_ARG, "eb_beam_output: bad arguments");
   if (points_per_beam < 2) return fail(EB_ERR_ARG, "eb_beam_output: points_per_beam must be at least 2");
@@ -1349,6 +1433,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
   CK(cudaMemsetAsync(h->d_relres, 0, sizeof(double) * S, st));
   const Dev& d = h->d;
   PhaseTimer& T = h->timer;
+  h->mid_step = true;
   T.begin(st);
 
   // ---- features of the learned start / of the captured samples (committed state)
@@ -1525,6 +1610,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
 
 static int commit_impl(eb_handle* h, const int32_t* mask, bool commit) {
   if (!h) return fail(EB_ERR_ARG, "null handle");
+  h->mid_step = false;
   int rc = upload_mask(h, h->d_mask, mask);
   if (rc) return rc;
   WsHost& ws = h->ws;

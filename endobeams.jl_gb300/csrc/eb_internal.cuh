@@ -78,6 +78,10 @@ struct Dev {
   double* Kt;                           // tangent, FP64
   float* Kt32;                          // tangent, FP32 copy
 
+  // ---- launch shapes (threads per block), chosen by eb_autotune among shapes whose
+  // results are bitwise identical
+  int beam_threads, contact_threads, gmat_threads, gvec_threads;
+
   // ---- DOF vectors (6 n_nodes)
   double *D, *Dd, *Ddd, *dD, *r, *fext1, *fextn, *Ti1, *Tin, *Tk1, *Tkn, *Tc1, *Tcn;
   uint8_t* fixed;    // dof is fixed
@@ -85,6 +89,7 @@ struct Dev {
 };
 
 constexpr int kThreads = 128;
+constexpr int kMaxElemThreads = 256;  // largest block of the element and contact kernels
 
 inline unsigned nblocks(int64_t n, int t = kThreads) { return (unsigned)((n + t - 1) / t); }
 

@@ -27,7 +27,7 @@ __device__ __forceinline__ V3 elem3(const double* f, int64_t ne, int64_t e) {
 
 // ------------------------------------------------------------------ assemble! element pass
 // One thread per element (compute_beams via assemble_beams.jl:21-48).
-__global__ void __launch_bounds__(kThreads) k_beam(Dev d, Gauss3 g) {
+__global__ void __launch_bounds__(kMaxElemThreads) k_beam(Dev d, Gauss3 g) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.n_elem) return;
   if (!d.active[d.elem_sim[e]]) return;
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kThreads) k_beam(Dev d, Gauss3 g) {
 }
 
 // One thread per contact element (compute_contact_beams via compute&assemble…:460-482).
-__global__ void __launch_bounds__(kThreads) k_contact(Dev d, Gauss3 g) {
+__global__ void __launch_bounds__(kMaxElemThreads) k_contact(Dev d, Gauss3 g) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.n_elem) return;
   if (!d.is_contact[e]) return;
@@ -84,10 +84,10 @@ __global__ void __launch_bounds__(kThreads) k_contact(Dev d, Gauss3 g) {
 }
 
 void launch_beam(const Dev& d, const Gauss3& g, cudaStream_t s) {
-  if (d.n_elem) k_beam<<<nblocks(d.n_elem), kThreads, 0, s>>>(d, g);
+  if (d.n_elem) k_beam<<<nblocks(d.n_elem, d.beam_threads), d.beam_threads, 0, s>>>(d, g);
 }
 void launch_contact(const Dev& d, const Gauss3& g, cudaStream_t s) {
-  if (d.n_elem) k_contact<<<nblocks(d.n_elem), kThreads, 0, s>>>(d, g);
+  if (d.n_elem) k_contact<<<nblocks(d.n_elem, d.contact_threads), d.contact_threads, 0, s>>>(d, g);
 }
 
 // ------------------------------------------------------------------ ordered block assembly
@@ -163,8 +163,8 @@ __global__ void k_gather_vec(Dev d, int with_contact) {
 }
 
 void launch_gather(const Dev& d, double alpha, bool with_contact, cudaStream_t s) {
-  if (d.nnzb) k_gather_mat<<<nblocks(d.nnzb * 36, 256), 256, 0, s>>>(d, alpha, with_contact ? 1 : 0);
-  if (d.n_dof) k_gather_vec<<<nblocks(d.n_dof, 256), 256, 0, s>>>(d, with_contact ? 1 : 0);
+  if (d.nnzb) k_gather_mat<<<nblocks(d.nnzb * 36, d.gmat_threads), d.gmat_threads, 0, s>>>(d, alpha, with_contact ? 1 : 0);
+  if (d.n_dof) k_gather_vec<<<nblocks(d.n_dof, d.gvec_threads), d.gvec_threads, 0, s>>>(d, with_contact ? 1 : 0);
 }
 
 // ------------------------------------------------------------------ predictor

@@ -190,6 +190,18 @@ int eb_get_memory(eb_handle *h, int64_t *device_bytes, int32_t *band_sims);
 /* Assembled global vectors of one simulation at n+1 (6 n_nodes each; NULL to skip). */
 int eb_get_forces(eb_handle *h, int32_t sim, double *Tint, double *Tk, double *Tc);
 
+/* Launch-shape autotuner (no counterpart in the reference): times the element, contact and
+ * assembly kernels on the current state at candidate block sizes (64/128/256 threads for the
+ * element and contact kernels, 128/256/512 for the two assembly kernels) and keeps the fastest.
+ * All candidates compute every value with the same operations in the same order, so results do
+ * not depend on the choice.  Call between steps (after eb_commit / eb_rollback; EB_ERR_STATE
+ * otherwise).  chosen (may be NULL) receives the four block sizes: element, contact, matrix
+ * assembly, vector assembly. */
+int eb_autotune(eb_handle *h, int32_t *chosen);
+/* Sets the four block sizes directly (multiples of 32; at most 256 for the element and contact
+ * kernels, 1024 for the assembly kernels). */
+int eb_set_launch_shapes(eb_handle *h, const int32_t *shapes);
+
 /* ---- output (src/IO/visualization_beams.jl) ----
  * recompute_at_gausspts_beams! (visualization_beams.jl:122-162) of one simulation's current
  * state: points_per_beam (>= 2) points per element at z = range(-1, 1, length = points_per_beam),

@@ -190,3 +190,38 @@ def test_graph_replay_matches_direct_launches(eb, scenes):
             res = eb.run_simulation(conf, p, inter)
             out[graph] = (conf.nodes.un.copy(), res.ks[0])
         assert np.array_equal(out[True][0], out[False][0]) and out[True][1] == out[False][1]
+
+
+def test_launch_shapes_change_no_result(eb, scenes):
+    """Every block size the autotuner may pick gives the same trajectory bit for bit
+    (ring on the SDF plane, contact from the first step), and eb_autotune refuses to
+    run between eb_step and eb_commit."""
+    def run(shapes, tune=False):
+        conf, p, inter = scenes.ring_drop(steps=12, height=2.2e-4)
+        p.tolerance_residual = 1e-5
+        p.autotune = tune
+        eng = eb.GpuSimulations([conf], p, [inter])
+        if shapes is not None:
+            eng.set_launch_shapes(*shapes)
+        res = eb.run_simulations([conf], p, [inter], engine=eng)
+        u = eng.state(0)["u"]
+        chosen = eng.autotune() if tune else None
+        eng.close()
+        return u, res.ks[0], chosen
+
+    base, ks, _ = run(None)
+    for shapes in [(64, 64, 128, 128), (256, 256, 512, 512), (128, 256, 256, 128)]:
+        u, k, _ = run(shapes)
+        assert k == ks and np.array_equal(u, base), shapes
+    u, k, chosen = run(None, tune=True)
+    assert k == ks and np.array_equal(u, base)
+    assert chosen["beam"] in (64, 128, 256) and chosen["contact"] in (64, 128, 256)
+    assert chosen["assembly_matrix"] in (128, 256, 512) and chosen["assembly_vector"] in (128, 256, 512)
+    conf, p, inter = scenes.ring_drop(steps=12, height=2.2e-4)
+    eng = eb.GpuSimulations([conf], p, [inter])
+    eng.step(np.full(1, p.initial_timestep))
+    with pytest.raises(eb.EbError, match="between steps"):
+        eng.autotune()
+    eng.commit()
+    eng.autotune()
+    eng.close()

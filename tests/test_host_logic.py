@@ -77,6 +77,21 @@ class _ScriptedEngine:
     def sync_nodes(self):
         pass
 
+    def autotune(self):
+        return {}
+
+    def vtk_open(self, dirs, points_per_beam=10):
+        self.calls.append(("vtk_open", tuple(dirs)))
+
+    def vtk_write(self, counter, step, t, mask=None):
+        m = np.ones(self.n, bool) if mask is None else np.asarray(mask, bool)
+        c, st, tt = (np.broadcast_to(x, (self.n,)) for x in (counter, step, t))
+        self.calls.append(("vtk", tuple((s, int(c[s]), int(st[s]), round(float(tt[s]), 12))
+                                        for s in range(self.n) if m[s])))
+
+    def vtk_close(self):
+        self.calls.append(("vtk_close",))
+
 
 class _ScriptedModel:
     """Stands in for the oracle's OracleModel in oracle.run_simulation."""
@@ -119,3 +134,53 @@ def test_time_loop_policy_matches_reference(eb, script):
     # same Δt sequence
     dts = [c[1][0] for c in eng.calls if c[0] == "dt"]
     assert np.allclose(dts, [d for (_, d) in [x for x in om.log if isinstance(x, tuple)]])
+
+
+def _reference_writes(script, p):
+    """The output schedule of run_simulation! (run_simulation.jl:30-32, 86-90), restated:
+    (write_counter, step, tⁿ) of every write_VTK call."""
+    import math
+    t, dt, succ, step, write_t = 0.0, p.initial_timestep, 0, 1, 0.0
+    ks = list(script)
+    out = [(0, 1, 0.0)]
+    counter = 1
+    while p.simulation_end_time - t > 1.0e-10:
+        t1 = t + dt
+        k = ks.pop(0)
+        if k > p.max_iterations:
+            dt /= 2
+            succ = 0
+            continue
+        succ += 1
+        if succ >= p.accelerate_after_success_it and k <= 8:
+            dt = min(dt * 1.5, p.max_timestep)
+            succ = 0
+        due = write_t + p.output_timestep
+        if t1 > due or math.isclose(t1, due, rel_tol=math.sqrt(np.finfo(float).eps), abs_tol=0.0):
+            out.append((counter, step, round(t, 12)))
+            counter += 1
+            write_t = t1
+        t = t1
+        step += 1
+    return out
+
+
+@pytest.mark.parametrize("every", [0.005, 0.02, 0.031])
+def test_vtk_output_schedule_matches_reference(eb, every, tmp_path):
+    """run_simulations with output_dir: the writes (counter, step, start time of the step)
+    per simulation are the reference's, including after rejected steps and Δt changes."""
+    script = [3, 3, 21, 3, 3, 3, 3, 3, 21, 21, 3, 3, 3, 3, 3, 3]
+    p = eb.SimulationParams(alpha=-0.05, beta=0.28, gamma=0.55, initial_timestep=0.01, min_timestep=1e-4,
+                            max_timestep=0.02, simulation_end_time=0.1, max_iterations=20,
+                            output_dir=str(tmp_path), output_timestep=every)
+    eng = _ScriptedEngine([script + [3] * 50, [3] * 80])
+    eb.run_simulations([None, None], p, engine=eng)
+    assert eng.calls[0] == ("vtk_open", (str(tmp_path / "sim_00000"), str(tmp_path / "sim_00001")))
+    assert eng.calls[-1] == ("vtk_close",)
+    got = {0: [], 1: []}
+    for c in eng.calls:
+        if c[0] == "vtk":
+            for sim, counter, step, t in c[1]:
+                got[sim].append((counter, step, t))
+    assert got[0] == _reference_writes(script + [3] * 50, p)
+    assert got[1] == _reference_writes([3] * 80, p)
