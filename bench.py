@@ -51,6 +51,12 @@ sys.path.insert(0, ROOT)
 # evaluated (profiles/beam_kernel_stent.md).
 F_ELEM_FP64 = 1702.0 + 3085.0 + 2 * 5987.0
 
+# Bytes one contact-element evaluation must read: both node records (X0, u, u_dot, w_dot: 12
+# doubles; R, dR: 18) = 480 B, the element's R_e0, l0, radius (88 B), its index words (13 B)
+# and the 27-coefficient quadratic B-spline stencil at each of the 3 Gauss points (648 B).
+# Elements in contact also write their 2.4 KB of tangents; those writes are not counted.
+B_CONTACT_ELEM = 480.0 + 88.0 + 13.0 + 648.0
+
 METRIC = "HHT steps/s & Newton iters/step, batched+learned vs plain"
 MODEL = os.path.join(ROOT, "endobeams.jl_gb300", "models", "warm_start_stents.npz")
 STENT_TOL_RES = 1e-7   # FP64 floor of the normalised residual reaches 1.4e-8 on the largest stents
@@ -478,6 +484,17 @@ def gpu_arm(args, rank, world):
                              "unit": "TFLOP/s", "frac": ach / peak_fp64, "traffic": None,
                              "avg_launch_ms": avg_beam_ms, "share_of_step": phase_ms["beam"] / sum(phase_ms.values())}
     peaks = _measured_peaks()
+    if launches["contact"] and tot["elem_evals"] and wl.kind == "stents":
+        # every stent element is a contact element: one contact evaluation per element evaluation
+        ach = B_CONTACT_ELEM * tot["elem_evals"] / (phase_ms["contact"] * 1e-3) / 1e9
+        hbm = peaks.get("hbm_gbs")
+        rooflines["contact"] = {"kernel": "k_contact (beam-to-SDF contact element, FP64)", "bound": "hbm",
+                                "achieved": ach, "peak": hbm,
+                                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else None, "unit": "GB/s",
+                                "frac": (ach / hbm) if hbm else None, "traffic": None,
+                                "algorithmic_bytes_per_element": B_CONTACT_ELEM,
+                                "note": "reads only; in-contact elements also write 2.4 KB each",
+                                "share_of_step": phase_ms["contact"] / sum(phase_ms.values())}
     if launches["krylov"] and wl.kind == "stents":
         per_iter = gmres_bytes_per_iter(wl, range(wl.count))
         iters_per_sim = tot["krylov"] / max(tot["sims"], 1)  # summed over the timed steps

@@ -351,6 +351,9 @@ struct eb_handle {
   double *d_cK = nullptr, *d_cC = nullptr, *d_cM = nullptr, *d_dt = nullptr;
   // solver
   SolverArgs sa{};
+  std::vector<SolverArgs> gclass;  // empty, or {wide-band class, two-CTAs-per-SM class}
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double *d_Dinv64 = nullptr;
   float* d_Dinv32 = nullptr;
   double* d_norms = nullptr;
@@ -435,7 +438,17 @@ int launch_solve(eb_handle* h, bool refactor, const int* refactor_src, PhaseTime
   T.mark(EB_PHASE_PRECOND, h->stream);
   const bool fp32 = h->P.precision == EB_PREC_MIXED;
   int threads = h->P.threads_per_sim > 0 ? h->P.threads_per_sim : 256;
-  CK(launch_gmres(h->sa, fp32, threads, h->stream));
+  if (h->gclass.size() == 2) {
+    // wide-band simulations on the handle's stream, the two-per-SM class beside them
+    CK(cudaEventRecord(h->ev_fork, h->stream));
+    CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+    CK(launch_gmres(h->gclass[0], fp32, threads, h->stream));
+    CK(launch_gmres(h->gclass[1], fp32, threads, h->side));
+    CK(cudaEventRecord(h->ev_join, h->side));
+    CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+  } else {
+    CK(launch_gmres(h->sa, fp32, threads, h->stream));
+  }
   T.mark(EB_PHASE_KRYLOV, h->stream);
   T.launches[EB_PHASE_KRYLOV] += 1;
   return EB_OK;
@@ -447,6 +460,12 @@ int solve(eb_handle* h, const int* mask) {
 }
 
 int record_iteration(eb_handle* h, bool refactor, PhaseTimer& T);
+
+// After a bounded bulk-copy wait ran out: band blocks are read from global memory from now on.
+void disable_staging(eb_handle* h) {
+  h->sa.stage_floats = 0;
+  for (SolverArgs& c : h->gclass) c.stage_floats = 0;
+}
 
 // Launches the captured corrector iteration (capturing it on first use).
 int run_iteration_graph(eb_handle* h, bool refactor) {
@@ -1053,6 +1072,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     CK(A.upload(&p_order, order));
     h->band = BandDev{p_band, p_boff, p_bw, p_pos, p_nat, p_work, p_li, p_ui, h->d_refactor, p_order};
     sa.band = h->band;
+    sa.cta_sim = p_order;
     h->need_refactor.assign(n_sims, 1);
     h->refactor_mask.assign(n_sims, 0);
     h->dt_at_factor.assign(n_sims, 0.0);
@@ -1068,6 +1088,48 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     if (h->any_band && p->stage_band) {
       sa.stage_floats = kPanel * (h->max_b + 1);
       if (gmres_smem_total(sa) > kGmresSmemLimit) sa.stage_floats = 0;
+    }
+    // Occupancy classes: the staging buffers are sized for the widest band of a launch, so
+    // one launch runs every CTA at the occupancy of the largest simulation.  Simulations
+    // whose own staged solve fits two CTAs per SM form a second launch with its own
+    // buffer size, on a second stream beside the first.
+    h->gclass.clear();
+    if (sa.stage_floats > 0) {
+      auto args_for = [&](const std::vector<int>& sims, bool two) {
+        SolverArgs c = sa;
+        int bmax = 0, nmax = 0;
+        for (int s2 : sims) {
+          bmax = std::max(bmax, h->band_b[s2]);
+          nmax = std::max<int>(nmax, (int)(6 * (h->node_off[s2 + 1] - h->node_off[s2])));
+        }
+        c.n_sims = (int)sims.size();
+        c.max_n = nmax;
+        c.stage_floats = kPanel * (bmax + 1);
+        c.x_in_smem = 1;
+        if (gmres_smem_total(c) > (two ? kGmresTwoPerSm : (size_t)200 * 1024)) c.x_in_smem = 0;
+        if (gmres_smem_total(c) > (two ? kGmresTwoPerSm : kGmresSmemLimit)) c.stage_floats = 0;
+        return c;
+      };
+      std::vector<int> big, small;
+      for (int s2 : order) {
+        SolverArgs one = sa;
+        one.x_in_smem = 0;
+        one.stage_floats = kPanel * (h->band_b[s2] + 1);
+        (h->band_b[s2] > 0 && gmres_smem_total(one) > kGmresTwoPerSm ? big : small).push_back(s2);
+      }
+      if (!big.empty() && !small.empty()) {
+        std::vector<int> cta(big);
+        cta.insert(cta.end(), small.begin(), small.end());
+        int* p_cta;
+        CK(A.upload(&p_cta, cta));
+        SolverArgs cb = args_for(big, false), cs = args_for(small, true);
+        cb.cta_sim = p_cta;
+        cs.cta_sim = p_cta + big.size();
+        h->gclass = {cb, cs};
+        CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+      }
     }
   }
 
@@ -1126,6 +1188,9 @@ int eb_destroy(eb_handle* h) {
   if (h->pin_active) cudaFreeHost(h->pin_active);
   if (h->pin_refactor) cudaFreeHost(h->pin_refactor);
   if (h->pin_norms) cudaFreeHost(h->pin_norms);
+  if (h->side) cudaStreamDestroy(h->side);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->t0) cudaEventDestroy(h->t0);
   if (h->t1) cudaEventDestroy(h->t1);
   delete h;
@@ -1235,9 +1300,11 @@ int eb_autotune(eb_handle* h, int32_t* chosen) {
     CK(err);
   }
   const double alpha = h->P.alpha;
+  // a candidate replaces the current shape only when it is at least 5% faster
   auto time_it = [&](int* knob, const int* cand, int nc, auto&& launch) -> cudaError_t {
-    float best = INFINITY;
-    int pick = *knob;
+    float best = INFINITY, t_cur = INFINITY;
+    const int cur = *knob;
+    int pick = cur;
     for (int c = 0; c < nc; ++c) {
       *knob = cand[c];
       launch();
@@ -1249,12 +1316,13 @@ int eb_autotune(eb_handle* h, int32_t* chosen) {
       if (e != cudaSuccess) return e;
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
+      if (cand[c] == cur) t_cur = ms;
       if (ms < best) {
         best = ms;
         pick = cand[c];
       }
     }
-    *knob = pick;
+    *knob = (best < 0.95f * t_cur) ? pick : cur;
     return cudaSuccess;
   };
   static const int kElem[3] = {64, 128, 256}, kGather[3] = {128, 256, 512};
@@ -1552,7 +1620,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
       if (q[4] < 0) {
         // a bulk-copy wait ran out in this solve: stop this simulation's Newton loop (the step
         // reports EB_SIM_WAIT_TIMEOUT) and read band blocks from global memory from now on
-        h->sa.stage_floats = 0;
+        disable_staging(h);
         h->graph_gen += 1;
         running[s] = 0;
         k[s] = P.max_iterations + 1;
@@ -1589,7 +1657,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
       // the step's solves are not trusted: report "not converged" (the caller rolls back)
       // and read band blocks from global memory from now on
       k[s] = P.max_iterations + 1;
-      h->sa.stage_floats = 0;
+      disable_staging(h);
       h->graph_gen += 1;
     }
     q.newton_iterations = iter[s];

@@ -86,7 +86,7 @@ __device__ __forceinline__ void cta_prec(const TM* __restrict__ Dinv, int64_t n0
 
 template <typename T>
 __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
-  const int s = a.band.order[blockIdx.x];
+  const int s = a.cta_sim[blockIdx.x];
   if (!a.active[s]) return;
   const int m = a.m;
   const int64_t n0 = a.sim_node_off[s];

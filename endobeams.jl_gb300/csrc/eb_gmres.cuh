@@ -5,7 +5,8 @@
 namespace eb {
 
 struct SolverArgs {
-  int n_sims;
+  int n_sims;            // CTAs of this launch (one simulation each)
+  const int* cta_sim;    // CTA -> simulation
   const int64_t* sim_node_off;
   const int* active;
   const int* row_ptr;
@@ -43,5 +44,9 @@ cudaError_t launch_gmres(const SolverArgs& a, bool fp32, int threads, cudaStream
 size_t gmres_smem(int m);
 size_t gmres_smem_total(const SolverArgs& a);  // dynamic shared memory of one launch
 constexpr size_t kGmresSmemLimit = 216 * 1024;  // leaves room for the kernel's static shared memory (ring, barriers)
+// Dynamic shared memory up to which two CTAs share an SM (228 KB per SM, minus the kernel's
+// static 4.4 KB and the 1 KB the hardware reserves, per CTA; 256 threads x 128 registers
+// also allow exactly two).
+constexpr size_t kGmresTwoPerSm = 108 * 1024;
 
 }  // namespace eb
