@@ -61,6 +61,11 @@ METRIC = "HHT steps/s & Newton iters/step, batched+learned vs plain"
 MODEL = os.path.join(ROOT, "endobeams.jl_gb300", "models", "warm_start_stents.npz")
 STENT_TOL_RES = 1e-7   # FP64 floor of the normalised residual reaches 1.4e-8 on the largest stents
 STENT_TOL_DISP = 1e-8
+# Inexact Newton: each Newton solve runs GMRES (FP32 inner, FP64 refinement) to 1e-4 of its
+# right-hand side instead of 1e-10.  Every step still converges to the same residual and
+# displacement tolerances (64 stents: 4.03 Newton iterations per step instead of 3.89, states
+# within 1e-14 m of the 1e-10 runs; 2.4x the HHT steps/s).
+NEWTON_FORCING = 1e-4
 
 
 def parse():
@@ -100,6 +105,7 @@ def stent_params(p, precision="mixed", warm="off"):
     # the stents' band LU costs ~0.1-1 s per factorisation on one SM: reuse it while GMRES needs <= 200
     # iterations (64 stents: 20.1 HHT steps/s never refactorising, 17.9 at 48, 14.5 at 16)
     p.refactor_its = 200
+    p.linear_tol = NEWTON_FORCING
     p.precision = precision
     p.warm_start = warm
     return p
@@ -159,6 +165,7 @@ class Workload:
             c, p, it = s.net_on_sphere(int(self.sides[i]), seed=1 + i, sdf=self.sdf)
             p.tolerance_residual = 1e-5
             p.tolerance_displacement = 1e-8
+            p.linear_tol = NEWTON_FORCING
             p.precision = self.precision
             return c, p, it
         v = self.variants[i]
@@ -183,6 +190,7 @@ class Workload:
             tol = (STENT_TOL_RES, STENT_TOL_DISP)
         return {"workload": w, "sims": self.count, "nodes": int(nodes), "elements": int(elements),
                 "resident_groups": groups, "tolerance_residual": tol[0], "tolerance_displacement": tol[1],
+                "linear_tol": NEWTON_FORCING,
                 "precision": self.precision, "warm_start": self.warm}
 
 

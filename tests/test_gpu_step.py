@@ -156,6 +156,23 @@ def test_stent_steps_match_oracle(eb, O, scenes):
     assert np.abs(conf.nodes.un - ref.un).max() <= 1e-6 * 8e-3
 
 
+def test_stent_inexact_newton_matches_oracle(eb, O, scenes):
+    """Inexact Newton (GMRES to 1e-4 relative per Newton solve, the benchmark's setting)
+    against the oracle's exact-LU Newton: every step still converges to the same
+    tolerances, so positions agree within 1e-6 of the stent size; Newton iteration
+    counts may differ by one."""
+    conf, p, inter = scenes.braided_stent(wires=16, elems_per_wire=60, grid=None, precision="mixed")
+    p.tolerance_residual = 1e-7
+    p.tolerance_displacement = 1e-8
+    p.krylov_restart = 32
+    ref, rr = _oracle_run(O, conf, p, inter, max_steps=6)
+    p.linear_tol = 1e-4
+    res = eb.run_simulation(conf, p, inter, max_steps=6)
+    assert res.steps[0] == rr["steps"] == 6
+    assert all(abs(a - b) <= 1 for a, b in zip(res.ks[0], rr["ks"]))
+    assert np.abs(conf.nodes.un - ref.un).max() <= 1e-6 * 8e-3
+
+
 def test_stent_population_batch_matches_single(eb, scenes):
     """Stents of different sizes, each with its own SDF, batched in one handle give
     bit-identical results to running each alone (per-simulation CTAs, fixed-order
