@@ -37,6 +37,7 @@ class EbParams(C.Structure):
         ("max_refinements", C.c_int32), ("threads_per_sim", C.c_int32), ("timing", C.c_int32),
         ("preconditioner", C.c_int32), ("refactor_its", C.c_int32), ("stage_band", C.c_int32),
         ("warm_start", C.c_int32), ("use_graph", C.c_int32),
+        ("forcing", C.c_int32), ("forcing_max", C.c_double),
     ]
 
 

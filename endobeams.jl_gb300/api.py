@@ -278,6 +278,9 @@ class SimulationParams:
     warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start)
     use_graph: bool = True           # replay each Newton iteration from a CUDA graph
     autotune: bool = True            # run_simulations: pick kernel block sizes after the first step
+    forcing: str = "fixed"           # "fixed": every solve to linear_tol; "ew": inexact Newton
+                                     # (Eisenstat-Walker forcing terms between linear_tol and forcing_max)
+    forcing_max: float = 1e-2
 
     def to_c(self) -> _lib.EbParams:
         p = _lib.default_params()
@@ -302,6 +305,10 @@ class SimulationParams:
             raise ValueError("warm_start must be 'off' or 'learned'")
         p.warm_start = 1 if self.warm_start == "learned" else 0
         p.use_graph = int(bool(self.use_graph))
+        if self.forcing not in ("fixed", "ew"):
+            raise ValueError("forcing must be 'fixed' or 'ew'")
+        p.forcing = 1 if self.forcing == "ew" else 0
+        p.forcing_max = float(self.forcing_max)
         return p
 
 

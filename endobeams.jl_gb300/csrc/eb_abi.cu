@@ -423,7 +423,18 @@ bool plan_refactor(eb_handle* h, const int* mask) {
 
 // Stream part of a linear solve; `refactor_src` is the host copy of the refactor mask
 // (pinned when the launches are captured into a graph).
-int launch_solve(eb_handle* h, bool refactor, const int* refactor_src, PhaseTimer& T) {
+// Solver arguments of one launch: corrector solves take the Eisenstat-Walker forcing term
+// (when enabled); predictor solves a fixed tolerance (forcing_max under EW).
+static SolverArgs solve_args(const eb_handle* h, const SolverArgs& base, bool corrector) {
+  SolverArgs a = base;
+  if (base.forcing && !corrector) {
+    a.forcing = 0;
+    a.tol = base.forcing_max;
+  }
+  return a;
+}
+
+int launch_solve(eb_handle* h, bool refactor, const int* refactor_src, PhaseTimer& T, bool corrector) {
   if (h->any_jacobi) {
     launch_block_jacobi(h->d, h->d_Dinv64, h->d_Dinv32, h->stream);
     T.launches[EB_PHASE_PRECOND] += 1;
@@ -442,21 +453,21 @@ int launch_solve(eb_handle* h, bool refactor, const int* refactor_src, PhaseTime
     // wide-band simulations on the handle's stream, the two-per-SM class beside them
     CK(cudaEventRecord(h->ev_fork, h->stream));
     CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
-    CK(launch_gmres(h->gclass[0], fp32, threads, h->stream));
-    CK(launch_gmres(h->gclass[1], fp32, threads, h->side));
+    CK(launch_gmres(solve_args(h, h->gclass[0], corrector), fp32, threads, h->stream));
+    CK(launch_gmres(solve_args(h, h->gclass[1], corrector), fp32, threads, h->side));
     CK(cudaEventRecord(h->ev_join, h->side));
     CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
   } else {
-    CK(launch_gmres(h->sa, fp32, threads, h->stream));
+    CK(launch_gmres(solve_args(h, h->sa, corrector), fp32, threads, h->stream));
   }
   T.mark(EB_PHASE_KRYLOV, h->stream);
   T.launches[EB_PHASE_KRYLOV] += 1;
   return EB_OK;
 }
 
-int solve(eb_handle* h, const int* mask) {
+int solve(eb_handle* h, const int* mask, bool corrector) {
   const bool any = plan_refactor(h, mask);
-  return launch_solve(h, any, h->refactor_mask.data(), h->timer);
+  return launch_solve(h, any, h->refactor_mask.data(), h->timer, corrector);
 }
 
 int record_iteration(eb_handle* h, bool refactor, PhaseTimer& T);
@@ -538,7 +549,7 @@ int record_iteration(eb_handle* h, bool refactor, PhaseTimer& T) {
   launch_apply_bc(d, st);
   T.mark(EB_PHASE_RESIDUAL, st);
   T.launches[EB_PHASE_RESIDUAL] += 3;
-  int rc = launch_solve(h, refactor, h->pin_refactor, T);
+  int rc = launch_solve(h, refactor, h->pin_refactor, T, true);
   if (rc) return rc;
   launch_global_corrector(d, st);
   launch_local_corrector(d, b, g, st);
@@ -578,6 +589,8 @@ int eb_default_params(eb_params* p) {
   p->stage_band = 1;
   p->warm_start = EB_WS_OFF;
   p->use_graph = 1;
+  p->forcing = EB_FORCING_FIXED;
+  p->forcing_max = 1e-2;
   return EB_OK;
 }
 
@@ -1027,6 +1040,13 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   sa.refs = h->d_refs;
   sa.relres = h->d_relres;
   sa.status = h->d_status;
+  if (p->forcing != EB_FORCING_FIXED && p->forcing != EB_FORCING_EW) return fail(EB_ERR_ARG, "eb_create: bad forcing mode");
+  if (p->forcing == EB_FORCING_EW && !(p->forcing_max > 0 && p->forcing_max < 1))
+    return fail(EB_ERR_ARG, "eb_create: forcing_max must lie in (0, 1)");
+  sa.forcing = p->forcing == EB_FORCING_EW ? 1 : 0;
+  sa.forcing_max = p->forcing_max;
+  CK(A.alloc(&sa.prev_bnorm, n_sims));
+  CK(A.alloc(&sa.prev_eta, n_sims));
   h->stats.assign(n_sims, eb_sim_stats{});
   h->h_norms.assign(5 * (size_t)n_sims, 0.0);
 
@@ -1454,7 +1474,7 @@ static int learned_start_check(eb_handle* h, const std::vector<int>& running, do
   launch_predictor_rhs(d, a, b, g, st);
   launch_apply_bc(d, st);
   T.launches[EB_PHASE_PREDICTOR] += 4;
-  int rc = solve(h, fb.data());
+  int rc = solve(h, fb.data(), false);
   if (rc) return rc;
   launch_global_predictor(d, b, g, st);
   launch_local_predictor(d, b, g, st);
@@ -1533,7 +1553,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     }
     if (any_plain) {
       CK(cudaMemcpyAsync(h->d_active, plain.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
-      rc = solve(h, plain.data());
+      rc = solve(h, plain.data(), false);
       if (rc) return rc;
     }
     if (any_try) {
@@ -1545,7 +1565,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     }
     CK(cudaMemcpyAsync(h->d_active, act.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
   } else {
-    rc = solve(h, act.data());
+    rc = solve(h, act.data(), false);
     if (rc) return rc;
   }
   launch_global_predictor(d, b, g, st);
@@ -1559,6 +1579,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     CK(cudaStreamSynchronize(st));
     T.resolve();
   }
+  if (h->sa.forcing) CK(cudaMemsetAsync(h->sa.prev_bnorm, 0, sizeof(double) * S, st));  // first corrector solve: forcing_max
   std::vector<double> res(S, INFINITY), dn(S, INFINITY);
   std::vector<int> running(S);
   for (int s = 0; s < S; ++s) running[s] = act[s] && (1 <= P.max_iterations);
@@ -1604,7 +1625,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
       if (rc) return rc;
     }
     first = false;
-    rc = solve(h, running.data());
+    rc = solve(h, running.data(), true);
     if (rc) return rc;
     launch_global_corrector(d, st);
     launch_local_corrector(d, b, g, st);

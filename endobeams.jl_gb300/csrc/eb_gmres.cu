@@ -156,8 +156,26 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   int its = 0, refs = 0, status = 0;
   if (!isfinite(bnorm)) status = 2;  // EB_SIM_NAN
 
+  // relative tolerance of this solve (inexact Newton, Eisenstat-Walker choice 2)
+  double rtol = a.tol;
+  if (a.forcing) {
+    const double prev = a.prev_bnorm[s], pe = a.prev_eta[s];
+    double eta = a.forcing_max;
+    if (prev > 0.0) {
+      const double q = bnorm / prev;
+      eta = 0.9 * q * q;
+      if (0.9 * pe * pe > 0.1) eta = fmax(eta, 0.9 * pe * pe);
+      eta = fmin(fmax(eta, a.tol), a.forcing_max);
+    }
+    rtol = eta;
+    __syncthreads();  // every thread has read the previous values
+    if (threadIdx.x == 0) {
+      a.prev_bnorm[s] = bnorm;
+      a.prev_eta[s] = eta;
+    }
+  }
   if (status == 0 && bnorm > 0.0) {
-    const double target = a.tol * bnorm;
+    const double target = rtol * bnorm;
     for (int ref = 0; ref < a.max_ref && rnorm > target && its < a.max_iter; ++ref) {
       // ---- one GMRES(m) cycle on the FP64 residual R
       const double beta = rnorm;

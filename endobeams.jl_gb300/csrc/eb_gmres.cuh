@@ -37,6 +37,12 @@ struct SolverArgs {
   int max_n;             // largest simulation, in DOFs
   int stage_floats;      // > 0: band blocks staged in shared memory, floats per buffer (32 (b_max + 1))
   int stage_test_extra;  // > 0: the first forward block waits for bytes no copy delivers (tests the bounded wait)
+  // inexact Newton: 0 fixed tolerance `tol`; 1 Eisenstat-Walker forcing term from this solve's
+  // right-hand side norm and the previous corrector solve's (per simulation, on the device)
+  int forcing;
+  double forcing_max;
+  double* prev_bnorm;    // per sim: right-hand side norm of the previous corrector solve (0: none this step)
+  double* prev_eta;      // per sim: its forcing term
 };
 
 void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream_t s);

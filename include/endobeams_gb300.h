@@ -86,7 +86,17 @@ typedef struct {
   int32_t use_graph;                      /* 1: each Newton iteration is one CUDA graph launch (captured once
                                              per handle and refactorisation variant); not with timing = 1,
                                              whose per-phase events need separate launches */
+  int32_t forcing;                        /* EB_FORCING_FIXED: every solve to linear_tol;
+                                             EB_FORCING_EW: inexact Newton, Eisenstat-Walker forcing terms */
+  double forcing_max;                     /* EB_FORCING_EW: largest relative tolerance of a solve (also the
+                                             predictor's); linear_tol is the smallest */
 } eb_params;
+
+/* Linear-solve tolerance per Newton iteration */
+#define EB_FORCING_FIXED 0  /* linear_tol for every solve (the reference's direct solve, approximated) */
+#define EB_FORCING_EW 1     /* η_k = 0.9 (‖F_k‖ / ‖F_k-1‖)², kept >= 0.9 η_k-1² when that exceeds 0.1,
+                               clamped to [linear_tol, forcing_max]; forcing_max for a step's first
+                               corrector solve and for the predictor (Eisenstat & Walker 1996, choice 2) */
 
 /* Newton start of each step */
 #define EB_WS_OFF 0      /* HHT predictor (predictor.jl:1-27) */

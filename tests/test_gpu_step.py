@@ -156,17 +156,21 @@ def test_stent_steps_match_oracle(eb, O, scenes):
     assert np.abs(conf.nodes.un - ref.un).max() <= 1e-6 * 8e-3
 
 
-def test_stent_inexact_newton_matches_oracle(eb, O, scenes):
-    """Inexact Newton (GMRES to 1e-4 relative per Newton solve, the benchmark's setting)
-    against the oracle's exact-LU Newton: every step still converges to the same
-    tolerances, so positions agree within 1e-6 of the stent size; Newton iteration
-    counts may differ by one."""
+@pytest.mark.parametrize("forcing", ["fixed", "ew"])
+def test_stent_inexact_newton_matches_oracle(eb, O, scenes, forcing):
+    """Inexact Newton — GMRES to 1e-4 relative per Newton solve, or Eisenstat-Walker
+    forcing terms in [1e-10, 1e-2] — against the oracle's exact-LU Newton: every step
+    still converges to the same tolerances, so positions agree within 1e-6 of the stent
+    size; Newton iteration counts may differ by one."""
     conf, p, inter = scenes.braided_stent(wires=16, elems_per_wire=60, grid=None, precision="mixed")
     p.tolerance_residual = 1e-7
     p.tolerance_displacement = 1e-8
     p.krylov_restart = 32
     ref, rr = _oracle_run(O, conf, p, inter, max_steps=6)
-    p.linear_tol = 1e-4
+    if forcing == "fixed":
+        p.linear_tol = 1e-4
+    else:
+        p.forcing, p.linear_tol, p.forcing_max = "ew", 1e-10, 1e-2
     res = eb.run_simulation(conf, p, inter, max_steps=6)
     assert res.steps[0] == rr["steps"] == 6
     assert all(abs(a - b) <= 1 for a, b in zip(res.ks[0], rr["ks"]))
