@@ -501,7 +501,9 @@ def gpu_arm(args, rank, world):
                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else None, "unit": "GB/s",
                                 "frac": (ach / hbm) if hbm else None, "traffic": None,
                                 "algorithmic_bytes_per_element": B_CONTACT_ELEM,
-                                "note": "reads only; in-contact elements also write 2.4 KB each",
+                                "note": "reads only; in-contact elements also write 2.4 KB each. The kernel is bound "
+                                        "by the FP64 pipe (75% active under ncu), not by HBM: "
+                                        "profiles/contact_kernel_stents16.md",
                                 "share_of_step": phase_ms["contact"] / sum(phase_ms.values())}
     if launches["krylov"] and wl.kind == "stents":
         per_iter = gmres_bytes_per_iter(wl, range(wl.count))
