@@ -207,9 +207,16 @@ def est_bytes(stats):
 
 
 def plan_groups(wl, budget):
-    """Greedy resident groups in population order under a device-byte budget."""
+    """Resident groups under a device-byte budget, filled in decreasing order of the
+    band-solve cost n (b + 6).  A group's Krylov phase lasts as long as its costliest
+    simulation's chain of band sweeps (one CTA each), so the costliest simulations share
+    one group and the later groups hold only cheaper ones (shorter critical paths)."""
+    def cost(i):
+        n, _, w, _, _ = wl.stats(i)
+        return n * (6 * w + 5 + 6)
+    order = sorted(range(wl.count), key=lambda i: (-cost(i), i))
     groups, cur, acc = [], [], 0
-    for i in range(wl.count):
+    for i in order:
         bts = est_bytes(wl.stats(i))
         if cur and acc + bts > budget:
             groups.append(cur)
