@@ -207,16 +207,14 @@ def est_bytes(stats):
 
 
 def plan_groups(wl, budget):
-    """Resident groups under a device-byte budget, filled in decreasing order of the
-    band-solve cost n (b + 6).  A group's Krylov phase lasts as long as its costliest
-    simulation's chain of band sweeps (one CTA each), so the costliest simulations share
-    one group and the later groups hold only cheaper ones (shorter critical paths)."""
-    def cost(i):
-        n, _, w, _, _ = wl.stats(i)
-        return n * (6 * w + 5 + 6)
-    order = sorted(range(wl.count), key=lambda i: (-cost(i), i))
+    """Greedy resident groups in population order under a device-byte budget.
+
+    Population order mixes costly and cheap stents in every group, so the costliest
+    ones (one CTA each, largest first) overlap with the cheap ones.  Filling the groups
+    in decreasing cost instead put the 552 costliest stents in one group, where they
+    queue in 3.6 waves on the 152 SMs: 97.7 instead of 192.6 HHT steps/s."""
     groups, cur, acc = [], [], 0
-    for i in order:
+    for i in range(wl.count):
         bts = est_bytes(wl.stats(i))
         if cur and acc + bts > budget:
             groups.append(cur)

@@ -27,10 +27,6 @@ def test_memory_estimate_and_groups():
     # a stent holds 0.1-0.8 GB (the 64-stent batch measured 17.3 GB; estimator 17.7 GB)
     assert all(0.05e9 < s < 1.5e9 for s in sizes), sizes
     groups = bench.plan_groups(wl, int(1.01 * max(sizes) * 3))
-    assert sorted(i for g in groups for i in g) == list(range(12))
+    assert sum(len(g) for g in groups) == 12 and [i for g in groups for i in g] == list(range(12))
     assert all(sum(sizes[i] for i in g) <= 1.01 * max(sizes) * 3 or len(g) == 1 for g in groups)
-    # costliest simulations first: every simulation of a group costs at least as much as any of a later group
-    cost = lambda i: wl.stats(i)[0] * (6 * wl.stats(i)[2] + 11)
-    for a, b in zip(groups, groups[1:]):
-        assert min(cost(i) for i in a) >= max(cost(i) for i in b)
     assert len(bench.plan_groups(wl, 10 ** 15)) == 1
