@@ -14,7 +14,8 @@ from ._lib import EbError, check, device_info, f64, i32, ptr
 from .api import (BeamElementSurface, Beams, BeamsConfiguration, BoundaryConditions, ConcentratedForce,
                   DiscreteSignedDistanceField, Encastre, GpuSimulations, ImposedDisplacement, InteractionProperties,
                   Loads, NodesBeams, PlaneSurface, RigidInteraction, RunResult, SimulationParams, SphereSurface,
-                  read_vtk_sdf, run_simulation, run_simulations)
+                  read_vtk_sdf, read_vtk_triangle_mesh, run_simulation, run_simulations,
+                  TriangulatedSurface)
 
 GAUSS = np.array([5 / 9, 8 / 9, 5 / 9, -np.sqrt(3 / 5), 0.0, np.sqrt(3 / 5)])
 
@@ -50,4 +51,5 @@ __all__ = [
     "BoundaryConditions", "InteractionProperties", "SphereSurface", "PlaneSurface", "DiscreteSignedDistanceField",
     "BeamElementSurface", "RigidInteraction", "SimulationParams", "run_simulation", "run_simulations",
     "GpuSimulations", "RunResult", "element_eval", "contact_eval", "device_info", "read_vtk_sdf", "EbError",
+    "read_vtk_triangle_mesh", "TriangulatedSurface",
 ]

@@ -104,6 +104,7 @@ SIGNATURES = {
     "eb_fp64_peak": (C.c_int, [P_d]),
     "eb_beam_output": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P_d]),
     "eb_autotune": (C.c_int, [C.c_void_p, P_i32]),
+    "eb_sdf_from_mesh": (C.c_int, [C.c_int64, P_d, C.c_int64, P_i64, P_i64, P_d, P_d, P_d]),
     "eb_set_launch_shapes": (C.c_int, [C.c_void_p, P_i32]),
     "eb_vtk_open": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.c_int32]),
     "eb_vtk_write": (C.c_int, [C.c_void_p, P_i32, P_i32, P_i32, P_d]),

@@ -201,6 +201,80 @@ class DiscreteSignedDistanceField:
     def from_grid(cls, values, origin, spacing, inside=True):
         return cls(None, inside, values=values, origin=origin, spacing=spacing)
 
+    @classmethod
+    def from_mesh(cls, positions, triangles, origin, spacing, dims, inside=True):
+        """Signed distance of a closed triangle mesh sampled on the grid, computed on the
+        device (eb_sdf_from_mesh): positive inside the mesh, as the reference's SDF files are
+        for bodies inside the surface.  ``triangles`` are 1-based like read_vtk_triangle_mesh's."""
+        V = f64(positions).reshape(-1, 3)
+        T = i64(triangles).reshape(-1, 3) - 1
+        d = i64([int(x) for x in dims])
+        o = f64(origin)
+        h = f64(np.broadcast_to(np.asarray(spacing, float), (3,)))
+        out = np.zeros(int(d[0] * d[1] * d[2]))
+        check(_lib.load().eb_sdf_from_mesh(len(V), ptr(V), len(T), ptr(T, C.c_int64), ptr(d, C.c_int64), ptr(o),
+                                           ptr(h), ptr(out)), "eb_sdf_from_mesh")
+        return cls.from_grid(out.reshape(int(d[2]), int(d[1]), int(d[0])), o, h, inside=inside)
+
+
+def read_vtk_triangle_mesh(file_path: str):
+    """read_vtk_triangle_mesh (read_input_files.jl:81-152): the POINTS (one per line) and
+    the 3-node cells of a legacy-VTK file; returns (positions list, 1-based triangles list)."""
+    nodes, tris = [], []
+    in_points = in_cells = False
+    n_points = n_cells = 0
+    with open(file_path) as fh:
+        for line in fh:
+            line = line.rstrip("\n")
+            if not line or line.startswith("#"):
+                continue
+            if "POINTS" in line:
+                in_points, n_points = True, int(line.split()[1])
+                continue
+            if in_points:
+                if len(nodes) < n_points:
+                    nodes.append([float(x) for x in line.split()])
+                if len(nodes) == n_points:
+                    in_points = False
+                continue
+            if "CELLS" in line:
+                in_cells, n_cells = True, int(line.split()[1])
+                continue
+            if in_cells:
+                cell = [int(x) for x in line.split()]
+                if cell[0] == 3:
+                    tris.append([c + 1 for c in cell[1:]])
+                if len(tris) == n_cells:
+                    break
+    return [np.array(p, float) for p in nodes], [np.array(t, np.int64) for t in tris]
+
+
+@dataclass
+class TriangulatedSurface:
+    """TriangulatedSurface(positions, triangles) (def_interactions.jl:46-49), 1-based triangles.
+
+    The reference declares it without contact functions.  Here it becomes a master
+    surface through its signed distance field, computed on the device at create on a
+    grid of `spacing` (default: 1/64 of the mesh's largest extent) padded by `margin`
+    cells; `inside` as for DiscreteSignedDistanceField."""
+    positions: Sequence
+    triangles: Sequence
+    spacing: Optional[float] = None
+    margin: int = 4
+    inside: bool = True
+
+    def grid(self):
+        """(origin, spacing, dims) of the SDF grid."""
+        V = f64(np.asarray(self.positions, float)).reshape(-1, 3)
+        lo, hi = V.min(0), V.max(0)
+        h = float(self.spacing) if self.spacing else float((hi - lo).max()) / 64
+        dims = np.ceil((hi - lo) / h).astype(int) + 2 * self.margin + 1
+        return lo - self.margin * h, h, dims
+
+    def to_sdf(self) -> "DiscreteSignedDistanceField":
+        o, h, dims = self.grid()
+        return DiscreteSignedDistanceField.from_mesh(self.positions, self.triangles, o, h, dims, inside=self.inside)
+
 
 def read_vtk_sdf(filename: str):
     """Legacy-VTK structured-points reader with the layout of read_vtk_sdf (read_input_files.jl:154-195)."""
@@ -376,7 +450,9 @@ class GpuSimulations:
                 d.surface = _lib.EB_SURFACE_PLANE
                 d.plane_axis = m.axis_index
                 d.plane_position = float(m.position)
-            elif isinstance(m, DiscreteSignedDistanceField):
+            elif isinstance(m, (DiscreteSignedDistanceField, TriangulatedSurface)):
+                if isinstance(m, TriangulatedSurface):
+                    m = m.to_sdf()
                 d.surface = _lib.EB_SURFACE_SDF
                 for i in range(3):
                     d.sdf_dims[i] = m.dims[i]

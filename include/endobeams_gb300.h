@@ -212,6 +212,16 @@ int eb_autotune(eb_handle *h, int32_t *chosen);
  * kernels, 1024 for the assembly kernels). */
 int eb_set_launch_shapes(eb_handle *h, const int32_t *shapes);
 
+/* Signed distance field of a closed triangle mesh (no counterpart in the reference, whose SDFs
+ * come precomputed from files, read_vtk_sdf; its vessel meshes are read by read_vtk_triangle_mesh,
+ * src/IO/read_input_files.jl:81-152).  verts: n_vert x 3; tris: n_tri x 3, 0-based; grid point
+ * (i, j, k) at origin + (i, j, k) * spacing, dims = (nx, ny, nz); out: nx*ny*nz values, x fastest
+ * (VTK order).  |value| = distance to the nearest triangle; positive inside the mesh (generalized
+ * winding number above 1/2, either orientation), negative outside: the convention of the
+ * reference's SDF files for bodies inside the surface (DiscreteSignedDistanceField, inside = true). */
+int eb_sdf_from_mesh(int64_t n_vert, const double *verts, int64_t n_tri, const int64_t *tris, const int64_t *dims,
+                     const double *origin, const double *spacing, double *out);
+
 /* ---- output (src/IO/visualization_beams.jl) ----
  * recompute_at_gausspts_beams! (visualization_beams.jl:122-162) of one simulation's current
  * state: points_per_beam (>= 2) points per element at z = range(-1, 1, length = points_per_beam),

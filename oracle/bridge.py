@@ -31,7 +31,13 @@ def scene_from_conf(conf, inter=None) -> O.Scene:
         m, p = inter.master, inter.properties
         sc.contact_props = (p.kn, p.mu, p.eps_t, p.eta_n)
         sc.contact_elems = np.asarray(inter.slave.contact_beams, np.int64)
-        if hasattr(m, "axis_index"):
+        if hasattr(m, "triangles"):  # TriangulatedSurface: the oracle's own mesh-to-SDF on the same grid
+            import mesh_oracle
+            o, h, dims = m.grid()
+            vals = mesh_oracle.sdf_from_mesh(np.asarray(m.positions, float), np.asarray(m.triangles) - 1, o, h, dims)
+            vals = vals.reshape(int(dims[2]), int(dims[1]), int(dims[0]))
+            sc.surface = dict(kind="sdf", field=vals if m.inside else -vals, x0=tuple(o), h=(h, h, h))
+        elif hasattr(m, "axis_index"):
             sc.surface = dict(kind="plane", axis=m.axis_index, position=float(m.position))
         elif hasattr(m, "values"):
             vals = np.asarray(m.values, float)
