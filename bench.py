@@ -111,10 +111,29 @@ def stent_params(p, precision="mixed", warm="off"):
     return p
 
 
-class Workload:
-    """A named workload: simulations built lazily in resident groups."""
+def shard(sizes, per_rank, rank, world):
+    """Indices of this rank's simulations: the population of per_rank x world simulations split
+    into equal-count shards by a greedy balance on size (largest first to the least-loaded rank
+    with room), returned in population order.  One rank gets the whole population."""
+    if world == 1:
+        return list(range(len(sizes)))
+    load = [0] * world
+    cnt = [0] * world
+    mine = []
+    for i in sorted(range(len(sizes)), key=lambda i: (-sizes[i], i)):
+        r = min((q for q in range(world) if cnt[q] < per_rank), key=lambda q: (load[q], q))
+        load[r] += sizes[i]
+        cnt[r] += 1
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
 
-    def __init__(self, name, precision=None, warm=None, count=None):
+
+class Workload:
+    """A named workload: simulations built lazily in resident groups; under torchrun each
+    rank builds its own shard of a population world times as large (weak scaling)."""
+
+    def __init__(self, name, precision=None, warm=None, count=None, rank=0, world=1):
         _pkg()
         from endobeams_gb300 import scenes
         self.scenes = scenes
@@ -124,7 +143,8 @@ class Workload:
             if name not in ("nets256", "nets16"):
                 raise SystemExit(f"unknown workload {name}")
             self.count = 256 if name == "nets256" else 16
-            self.sides = scenes.net_sides(256, seed=0)[:self.count]
+            sides = scenes.net_sides(max(256, self.count * world), seed=0)[:self.count * world]
+            self.sides = [sides[i] for i in shard(list(sides), self.count, rank, world)]
             self.precision = precision or "fp64"
             self.warm = "off"
             self.sdf = None
@@ -137,7 +157,9 @@ class Workload:
                 self.variants = [("custom", int(m.group(1)), int(m.group(2)))]
             elif name.startswith("stents"):
                 n = count or int(name[len("stents"):] or 1024)
-                self.variants = scenes.stent_variants(1024, seed=2)[:n]
+                allv = scenes.stent_variants(max(1024, n * world), seed=2)[:n * world]
+                self.variants = [allv[i] for i in shard([v["wires"] * v["elems_per_wire"] for v in allv], n, rank,
+                                                        world)]
             else:
                 raise SystemExit(f"unknown workload {name}")
             self.count = len(self.variants)
@@ -446,7 +468,7 @@ def gmres_bytes_per_iter(wl, idx):
 def gpu_arm(args, rank, world):
     eb = _pkg()
     from endobeams_gb300 import _lib
-    wl = Workload(args.workload, args.precision, args.warm_start, args.count)
+    wl = Workload(args.workload, args.precision, args.warm_start, args.count, rank=rank, world=world)
     n_gpu, gname = eb.device_info()
     if n_gpu < 1:
         raise SystemExit("no CUDA device")

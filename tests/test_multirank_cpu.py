@@ -1,6 +1,7 @@
-"""The multi-GPU helpers of bench.py (weak scaling: every rank runs its own
-copy of the workload; the only collectives are a barrier and a max over
-ranks) exercised with two gloo ranks on the CPU."""
+"""The multi-GPU helpers of bench.py (weak scaling: every rank simulates its own
+shard of a population world times as large, balanced on element counts; the
+only collectives are a barrier and a max over ranks) exercised with two gloo
+ranks on the CPU."""
 import os
 import socket
 import sys
@@ -26,7 +27,9 @@ def _worker(rank, world, port, q):
     r, w = bench.dist_init()
     bench.barrier(w)
     mx = bench.allreduce_max(float(10 * (r + 1)), w)
-    q.put((r, w, mx))
+    wl = bench.Workload("stents64", rank=r, world=w)
+    shard = [tuple(sorted(v.items())) for v in wl.variants]
+    q.put((r, w, mx, shard))
     import torch.distributed as dist
     dist.destroy_process_group()
 
@@ -39,8 +42,18 @@ def test_two_gloo_ranks_barrier_and_max():
     procs = [mp.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
-    out = sorted(q.get(timeout=120) for _ in range(2))
+    out = sorted((q.get(timeout=300) for _ in range(2)), key=lambda x: x[0])
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    assert out == [(0, 2, 20.0), (1, 2, 20.0)]
+    assert [o[:3] for o in out] == [(0, 2, 20.0), (1, 2, 20.0)]
+    # shards: 64 stents each, disjoint, together the first 128 of the population, balanced
+    sys.path.insert(0, ROOT)
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from endobeams_gb300 import scenes
+    pop = [tuple(sorted(v.items())) for v in scenes.stent_variants(128, seed=2)]
+    a, b = out[0][3], out[1][3]
+    assert len(a) == len(b) == 64 and not set(a) & set(b) and sorted(a + b) == sorted(pop)
+    elems = lambda sh: sum(dict(v)["wires"] * dict(v)["elems_per_wire"] for v in sh)
+    assert abs(elems(a) - elems(b)) <= 0.02 * max(elems(a), elems(b))
