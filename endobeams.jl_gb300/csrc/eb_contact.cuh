@@ -307,37 +307,46 @@ EB_DEV void contact_element(const ContactIn& in, const Gauss3& gs, const Contact
     M3 auxK = (kn * dpn) * nn + (kn * pn) * d2g - outer(deta_n * udn, dg);
     M3 aux1 = outer(((-mureg) * kn * dpn) * udt, dg);
     M3 aux2 = ((-mureg) * kn * pn) * (I3 - (1 / (udt2 + eps_t)) * outer(udt, udt));
+    // The reference's ∂u̇ₙ/∂d = aux Rⱼ + nn D⁰ⱼ, ∂u̇ₜ/∂d = D⁰ⱼ - ∂u̇ₙ/∂d and ∂u̇ₜ/∂u̇ = Rⱼ - nn Rⱼ,
+    // substituted and collected (14 products instead of 32):
+    //   Kfcⱼ = A1 Rⱼ + A2 D⁰ⱼ,  Cfcⱼ = A2 Rⱼ,
+    //   A1 = auxK + aux1 - (ηₙ I + aux2) aux,  A2 = aux2 - aux2 nn - ηₙ nn.
+    M3 eta_aux2 = aux2;
+    eta_aux2.a[0] += eta_n; eta_aux2.a[4] += eta_n; eta_aux2.a[8] += eta_n;
+    const M3 A1 = (auxK + aux1) - eta_aux2 * aux;
+    const M3 A2 = aux2 - (aux2 * nn + eta_n * nn);
     M3 Kfc[4], Cfc[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      M3 dun_d = aux * RHR[j] + nn * du0[j];
-      M3 dut_d = du0[j] - dun_d;
-      M3 dut_v = RHR[j] - nn * RHR[j];
-      Kfc[j] = auxK * RHR[j] - eta_n * dun_d + (aux1 * RHR[j] + aux2 * dut_d);
-      Cfc[j] = ((-eta_n) * nn) * RHR[j] + aux2 * dut_v;
+      Kfc[j] = A1 * RHR[j] + A2 * du0[j];
+      Cfc[j] = A2 * RHR[j];
     }
     // accumulate (:332-370), one row block at a time:
     //   t₁ + t₃ (:128-155, :186-209): Rₑ[-S(H₁ⁱᵀ𝓕ᶜ) + H₁ⁱᵀS(𝓕ᶜ)] Gʲ Rₑᵀ, j = 1,2,4 (t^{i3} = -t^{i1});
-    //   t₂ row i from ReGᵢ and SFPⱼ (row 3 is minus row 1)
+    //   t₂ row i from ReGᵢ and SFPⱼ.
+    // H₁¹ + H₁³ = I (N₁ + N₂ = 1), so row block 3 is row block 1's complement: its t₁+t₃ and
+    // t₂ are minus row 1's, and its Rₑ H₁³ Rₑᵀ = I - Rₑ H₁¹ Rₑᵀ gives Kᶜ/Cᶜ terms Kfcⱼ - t₄¹ʲ.
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
+      if (i == 2) continue;  // formed with row block 0
       M3 Li = Re * (mulTN(H1[i], SFc) - skew(mulTv(H1[i], Fc)));
       const M3 t13_1 = Li * G1ReT, t13_2 = Li * G2ReT, t13_4 = Li * G4ReT;
       const M3& ReGi = (i == 1) ? ReG2 : (i == 3) ? ReG4 : ReG1;
-      M3 t2_1 = (i == 0 || i == 2) ? N7l2 * (Re * A1Fr) - ReG1 * SFP1 : -(ReGi * SFP1);
-      M3 t2_2 = -(ReGi * SFP2), t2_4 = -(ReGi * SFP4);
-      if (i == 2) {
-        t2_1 = -t2_1;
-        t2_2 = -t2_2;
-        t2_4 = -t2_4;
-      }
+      const M3 t2_1 = (i == 0) ? N7l2 * (Re * A1Fr) - ReG1 * SFP1 : -(ReGi * SFP1);
+      const M3 t2_2 = -(ReGi * SFP2), t2_4 = -(ReGi * SFP4);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        M3 t4 = mulTN(RHR[i], Kfc[j]);
-        M3 t13v = (j == 0) ? t13_1 : (j == 1) ? t13_2 : (j == 2) ? -t13_1 : t13_4;
-        M3 t2v = (j == 0) ? t2_1 : (j == 1) ? t2_2 : (j == 2) ? -t2_1 : t2_4;
-        acc_block(out.K, i, j, wg, (t13v + t2v) + t4);
-        acc_block(out.C, i, j, wg, mulTN(RHR[i], Cfc[j]));
+        const M3 t4 = mulTN(RHR[i], Kfc[j]);
+        const M3 t13v = (j == 0) ? t13_1 : (j == 1) ? t13_2 : (j == 2) ? -t13_1 : t13_4;
+        const M3 t2v = (j == 0) ? t2_1 : (j == 1) ? t2_2 : (j == 2) ? -t2_1 : t2_4;
+        const M3 tc = mulTN(RHR[i], Cfc[j]);
+        const M3 t12 = t13v + t2v;
+        acc_block(out.K, i, j, wg, t12 + t4);
+        acc_block(out.C, i, j, wg, tc);
+        if (i == 0) {
+          acc_block(out.K, 2, j, wg, (Kfc[j] - t4) - t12);
+          acc_block(out.C, 2, j, wg, Cfc[j] - tc);
+        }
       }
     }
   }
