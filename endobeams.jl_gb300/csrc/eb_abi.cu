@@ -317,6 +317,31 @@ struct IterGraph {
 };
 
 struct eb_handle {
+  // Releases the streams, events, graphs, pinned mirrors and output writer; the arena and
+  // the warm-start buffers free their device memory in their own destructors.
+  ~eb_handle() {
+    if (vtk) {
+      std::string err;
+      vtk_close(vtk, err);
+    }
+    if (stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+    timer.destroy();
+    for (auto& G : graph) {
+      if (G.exec) cudaGraphExecDestroy(G.exec);
+      G.timer.destroy();
+    }
+    if (pin_active) cudaFreeHost(pin_active);
+    if (pin_refactor) cudaFreeHost(pin_refactor);
+    if (pin_norms) cudaFreeHost(pin_norms);
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+  }
   bool mid_step = false;  // eb_step ran and neither eb_commit nor eb_rollback followed yet
   PhaseTimer timer;
   WsHost ws;
@@ -1190,30 +1215,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
 }
 
 int eb_destroy(eb_handle* h) {
-  if (!h) return EB_OK;
-  if (h->vtk) {
-    std::string err;
-    vtk_close(h->vtk, err);
-    h->vtk = nullptr;
-  }
-  if (h->stream) {
-    cudaStreamSynchronize(h->stream);
-    cudaStreamDestroy(h->stream);
-  }
-  h->timer.destroy();
-  for (auto& G : h->graph) {
-    if (G.exec) cudaGraphExecDestroy(G.exec);
-    G.timer.destroy();
-  }
-  if (h->pin_active) cudaFreeHost(h->pin_active);
-  if (h->pin_refactor) cudaFreeHost(h->pin_refactor);
-  if (h->pin_norms) cudaFreeHost(h->pin_norms);
-  if (h->side) cudaStreamDestroy(h->side);
-  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-  if (h->ev_join) cudaEventDestroy(h->ev_join);
-  if (h->t0) cudaEventDestroy(h->t0);
-  if (h->t1) cudaEventDestroy(h->t1);
-  delete h;
+  delete h;  // ~eb_handle releases everything, also on a failed eb_create
   return EB_OK;
 }
 
