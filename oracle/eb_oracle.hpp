@@ -1,5 +1,5 @@
 // ORACLE — test infrastructure only (tests/, smoke() and bench.py's CPU
-// baseline use it as the checker).  Never linked into, or called by, the
+// baseline use it to check the device results).  Never linked into, or called by, the
 // product library.
 //
 // Literal FP64 restatement of EndoBeams.jl's per-Newton-iteration hot path.

@@ -1,6 +1,6 @@
 """CPU restatement of the learned warm start's per-node MLP (test infrastructure).
 
-This is the checker for the device network kernels: forward pass, mean
+This checks the device network kernels: forward pass, mean
 squared error loss and its gradient, in float64 numpy, with the weights
 rounded to bfloat16 exactly as the device kernels read them (round to
 nearest even of the float32 value) and the biases kept in float32.

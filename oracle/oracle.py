@@ -2,8 +2,8 @@
 
 CPU FP64 restatement of EndoBeams.jl's time step (HHT-α predictor + Newton
 corrector), used by ``tests/``, ``__graft_entry__.smoke()`` and the CPU
-baseline arm of ``bench.py`` as the checker.  The product library never
-imports this module.
+baseline arm of ``bench.py`` to check the device results.  The product
+library never imports this module.
 
 The element, contact and nodal-rotation arithmetic runs in the C++ library
 ``oracle/_build/liboracle_eb.so`` (a literal restatement, see the .cpp
