@@ -13,7 +13,7 @@ node's displacement, velocity, acceleration, angular velocity and acceleration,
 the signed distance and its gradient at the node, and, for its first two beam
 neighbours j, u_j − u_i, u̇_j − u̇_i, φ_j and ∇φ_j.
 
-Plain Newton stays the judge: every step still iterates to the same
+Plain Newton stays the arbiter: every step still iterates to the same
 tolerances, and a simulation whose learned start has a larger first residual
 than the HHT predictor's right-hand side falls back to the predictor for that
 step.  Training data come from the plain solver itself (eb_ws_capture).

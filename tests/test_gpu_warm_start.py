@@ -2,7 +2,7 @@
 training with the library's own kernels, the per-simulation fallback to the
 HHT predictor, and what the trained network gains over the method without it.
 
-Plain Newton stays the judge: with or without the learned start every step
+Plain Newton stays the arbiter: with or without the learned start every step
 iterates to the same tolerances, so trajectories agree within the Newton
 tolerance (checked at 1e-6 of the structure size)."""
 import json
