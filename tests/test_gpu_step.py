@@ -213,6 +213,35 @@ def test_graph_replay_matches_direct_launches(eb, scenes):
         assert np.array_equal(out[True][0], out[False][0]) and out[True][1] == out[False][1]
 
 
+def test_two_occupancy_classes_graph_matches_direct_and_single(eb, scenes):
+    """A 48-wire stent (wide band: one CTA per SM) and a 16-wire stent (two per SM) in
+    one handle: the GMRES launch splits into two classes on two streams.  Replayed from
+    graphs (forked and joined inside the capture) or launched directly, and each stent
+    alone, the trajectories are bit for bit the same."""
+    def mk(wires):
+        c, p, it = scenes.stent_variant(dict(wires=wires, R=4e-3, pitch_deg=45.0, elems_per_wire=80,
+                                             cyl_frac=0.9), tol=1e-7)
+        p.krylov_restart = 32
+        p.tolerance_displacement = 1e-8
+        p.linear_tol = 1e-4
+        return c, p, it
+
+    def run(wires_list, graph):
+        built = [mk(w) for w in wires_list]
+        p = built[0][1]
+        p.use_graph = graph
+        confs = [b[0] for b in built]
+        res = eb.run_simulations(confs, p, [b[2] for b in built], max_steps=3)
+        return [c.nodes.un.copy() for c in confs], res.ks
+
+    both_graph = run([48, 16], True)
+    both_direct = run([48, 16], False)
+    alone = [run([48], True), run([16], True)]
+    for s in range(2):
+        assert np.array_equal(both_graph[0][s], both_direct[0][s]) and both_graph[1][s] == both_direct[1][s]
+        assert np.array_equal(both_graph[0][s], alone[s][0][0]) and both_graph[1][s] == alone[s][1][0]
+
+
 def test_launch_shapes_change_no_result(eb, scenes):
     """Every block size the autotuner may pick gives the same trajectory bit for bit
     (ring on the SDF plane, contact from the first step), and eb_autotune refuses to
