@@ -184,3 +184,25 @@ def test_vtk_output_schedule_matches_reference(eb, every, tmp_path):
                 got[sim].append((counter, step, t))
     assert got[0] == _reference_writes(script + [3] * 50, p)
     assert got[1] == _reference_writes([3] * 80, p)
+
+
+def test_plane_axis_and_output_dirs(eb, tmp_path):
+    assert eb.PlaneSurface(0.0, "x").axis_index == 0 and eb.PlaneSurface(1.0, "Z").axis_index == 2
+    assert eb.PlaneSurface(0.0, 1).axis_index == 1
+    with pytest.raises(ValueError):
+        eb.PlaneSurface(0.0, "w").axis_index
+    from endobeams_gb300 import api
+    assert api.output_dirs(str(tmp_path), 1) == [str(tmp_path)]
+    assert api.output_dirs(str(tmp_path), 3)[2] == str(tmp_path / "sim_00002")
+
+
+def test_triangulated_surface_grid_covers_the_mesh(eb):
+    V = np.array([[0, 0, 0], [2, 0, 0], [0, 1, 0], [0, 0, 0.5]], float)
+    T = np.array([[1, 2, 3], [1, 2, 4], [1, 3, 4], [2, 3, 4]])
+    ts = eb.TriangulatedSurface(V, T, spacing=0.1, margin=2)
+    o, h, dims = ts.grid()
+    assert h == 0.1 and np.allclose(o, [-0.2, -0.2, -0.2])
+    hi = o + (dims - 1) * h
+    assert np.all(hi >= V.max(0) + 2 * h - 1e-12)
+    ts2 = eb.TriangulatedSurface(V, T)  # default spacing: 1/64 of the largest extent
+    assert ts2.grid()[1] == pytest.approx(2.0 / 64)
