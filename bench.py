@@ -23,10 +23,10 @@ Workloads (synthetic, seeded; no dataset):
             U(±0.5 mm), r = 0.1 mm, E = 100 GPa, gravity, dropped on a sphere
             R = 15 mm given as a 128³ SDF at 0.3 mm; mu = 0.2, dt = 5e-5 s.
 
-Under torchrun (N > 1) every rank runs its own full copy of the workload on
-its GPU (weak scaling; simulations are independent, no collective in the
-data path); the timed region is bracketed by barriers and the slowest rank's
-time is reported.
+Under torchrun (N > 1) every rank binds the GPU of its local rank and
+simulates its own shard of a population N times as large (weak scaling;
+simulations are independent, no collective in the data path); the timed
+region is bracketed by barriers and the slowest rank's time is reported.
 """
 from __future__ import annotations
 
@@ -48,7 +48,7 @@ sys.path.insert(0, ROOT)
 # FP64 floating-point operations the device beam kernel executes per element
 # evaluation: 1,702 DADD + 3,085 DMUL + 5,987 DFMA (FMA = 2) counted by ncu's
 # SASS counters on a launch in which every element of a 48-wire stent is
-# evaluated (profiles/beam_kernel_stent.md).
+# evaluated.
 F_ELEM_FP64 = 1702.0 + 3085.0 + 2 * 5987.0
 
 # Bytes one contact-element evaluation must read: both node records (X0, u, u_dot, w_dot: 12
@@ -59,7 +59,15 @@ B_CONTACT_ELEM = 480.0 + 88.0 + 13.0 + 648.0
 
 METRIC = "HHT steps/s & Newton iters/step, batched+learned vs plain"
 MODEL = os.path.join(ROOT, "endobeams.jl_gb300", "models", "warm_start_stents.npz")
-STENT_TOL_RES = 1e-7   # FP64 floor of the normalised residual reaches 1.4e-8 on the largest stents
+# Newton tolerances of the stents.  The configurations ask for 1e-8.  The normalised residual of
+# the reference's algorithm has an FP64 floor that grows as the elements get shorter (rounding
+# of the element forces against the small contact and inertial loads; measured with the oracle:
+# 2e-9 at 0.15 mm elements, 1e-8 at 0.094 mm, 2.4e-8 at 0.071 mm); a stent whose floor is above
+# its tolerance never converges.  Stents with elements of at least 0.12 mm (floor <= 5e-9) run
+# at 1e-8, shorter-element stents at 1e-7; the displacement tolerance is 1e-8 for all.
+STENT_TOL_RES = 1e-8
+STENT_TOL_RES_SHORT = 1e-7
+STENT_ELEM_1E8 = 0.12e-3
 STENT_TOL_DISP = 1e-8
 # Inexact Newton: each Newton solve runs GMRES (FP32 inner, FP64 refinement) to 1e-4 of its
 # right-hand side instead of 1e-10.  Every step still converges to the same residual and
@@ -71,16 +79,19 @@ NEWTON_FORCING = 1e-4
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="stents1024")
     ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
     ap.add_argument("--warm-start", default=None, choices=[None, "off", "learned"])
     ap.add_argument("--count", type=int, default=None, help="population size override (stents)")
     ap.add_argument("--mem-frac", type=float, default=0.75, help="device memory fraction per resident group")
-    ap.add_argument("--cpu-sample", type=int, default=2, help="simulations in the CPU-baseline sample")
-    ap.add_argument("--cpu-steps", type=int, default=3, help="steps per simulation in the CPU-baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=2, help="simulations in the CPU-baseline sample of the GPU arm")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="steps per simulation in that CPU-baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=64,
+                    help="--impl reference: simulations spread over the population, each warmed up and timed "
+                         "over the same step window as the GPU arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-batch and single-stent legs")
@@ -96,6 +107,13 @@ def parse():
 def _pkg():
     import __graft_entry__ as g
     return g.load_package()
+
+
+def stent_tol_res(conf):
+    """Residual tolerance of one stent: 1e-8 unless its mean element is shorter than 0.12 mm."""
+    X, c = conf.nodes.X0, conf.beams.conn
+    le = float(np.linalg.norm(X[c[:, 1]] - X[c[:, 0]], axis=1).mean())
+    return STENT_TOL_RES if le >= STENT_ELEM_1E8 else STENT_TOL_RES_SHORT
 
 
 def stent_params(p, precision="mixed", warm="off"):
@@ -165,6 +183,7 @@ class Workload:
             self.count = len(self.variants)
             self.precision = precision or "mixed"
             self.warm = warm or ("learned" if (name.startswith("stents") and os.path.exists(MODEL)) else "off")
+        self.tol_res = {}  # per simulation index: its residual tolerance (stents)
 
     def stats(self, i):
         """(nodes, elements, RCM half bandwidth in nodes, SDF points, Krylov restart) of simulation i (cached)."""
@@ -197,7 +216,12 @@ class Workload:
             c, p, it = s.braided_stent(wires=v[1], elems_per_wire=v[2], grid=None)
         else:
             c, p, it = s.stent_variant(v)
+        self.tol_res[i] = stent_tol_res(c)
         return c, stent_params(p, self.precision, self.warm), it
+
+    @property
+    def n_tol8(self):
+        return sum(1 for t in self.tol_res.values() if t == STENT_TOL_RES)
 
     def describe(self, nodes, elements, groups):
         if self.kind == "nets":
@@ -209,7 +233,8 @@ class Workload:
         else:
             w = (f"{self.name}: {self.count} braided stents (seed 2; wires {{16,24,32,48}}, R U[3,5] mm, pitch "
                  f"U[35,55] deg, U{{100..400}} elements/wire, own cylinder SDF at 0.1 mm), dt=1e-5")
-            tol = (STENT_TOL_RES, STENT_TOL_DISP)
+            tol = (f"1e-8 (elements >= 0.12 mm: {self.n_tol8} sims), 1e-7 (shorter: {self.count - self.n_tol8})",
+                   STENT_TOL_DISP)
         return {"workload": w, "sims": self.count, "nodes": int(nodes), "elements": int(elements),
                 "resident_groups": groups, "tolerance_residual": tol[0], "tolerance_displacement": tol[1],
                 "linear_tol": NEWTON_FORCING,
@@ -359,6 +384,8 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
         params.warm_start = warm
     params.timing = True
     eng = eb.GpuSimulations(confs, params, inters)
+    if wl.kind == "stents":
+        eng.set_tolerances(residual=[wl.tol_res[i] for i in idx])
     if params.warm_start == "learned":
         from endobeams_gb300 import warm_start as W
         eng.set_warm_start(W.WarmStartModel.load(MODEL))
@@ -533,8 +560,7 @@ def gpu_arm(args, rank, world):
                                 "frac": (ach / hbm) if hbm else None, "traffic": None,
                                 "algorithmic_bytes_per_element": B_CONTACT_ELEM,
                                 "note": "reads only; in-contact elements also write 2.4 KB each. The kernel is bound "
-                                        "by the FP64 pipe (75% active under ncu), not by HBM: "
-                                        "profiles/contact_kernel_stents16.md",
+                                        "by the FP64 pipe (75% active under ncu on 16 stents), not by HBM",
                                 "share_of_step": phase_ms["contact"] / sum(phase_ms.values())}
     if launches["krylov"] and wl.kind == "stents":
         per_iter = gmres_bytes_per_iter(wl, range(wl.count))
@@ -552,7 +578,7 @@ def gpu_arm(args, rank, world):
     out = {
         "metric": METRIC if wl.kind == "stents" else "HHT steps/s (whole job), batched plain Newton",
         "value": value, "unit": "HHT steps/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
-        "ms_per_step": tot["ms"] / len(groups) / max(steps, 1), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": tot["ms"] / max(steps, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if wl.precision == "fp64" else "f64+f32-krylov", "data": "synthetic",
         "config": dict(wl.describe(tot["nodes"], tot["elements"], len(groups)),
                        l2="state, band and staging arrays exceed L2 (129 MB) each step", device=gname,
@@ -602,25 +628,32 @@ def _measured_peaks():
 
 # ------------------------------------------------------------------ CPU arms (oracle restatement)
 
-def cpu_rate(workload, precision, sample, steps, cores):
-    """Oracle HHT steps/s on `sample` simulations x `steps` steps with `cores` spawned processes.
-
-    Model construction (pattern, SDF prefilter) happens before each worker's clock starts."""
-    idx = list(range(sample))
+def cpu_rate(workload, precision, idx, steps, cores, warmup=0):
+    """Oracle HHT steps/s on the simulations `idx` of the workload with `cores` spawned processes:
+    each simulation takes `warmup` untimed steps, then `steps` timed ones (the GPU arm's step
+    window).  Model construction (pattern, SDF prefilter) and the warm-up happen outside the
+    clock; the rate is all timed steps over the busiest process's timed seconds."""
+    idx = list(idx)
     chunks = [idx[i::cores] for i in range(cores) if idx[i::cores]]
     if len(chunks) == 1:
-        res = [_timed_chunk((workload, precision, chunks[0], steps))]
+        res = [_timed_chunk((workload, precision, chunks[0], steps, warmup))]
     else:
         ctx = mp.get_context("spawn")
         with ctx.Pool(len(chunks)) as pool:
-            res = pool.map(_timed_chunk, [(workload, precision, c, steps) for c in chunks])
+            res = pool.map(_timed_chunk, [(workload, precision, c, steps, warmup) for c in chunks])
     done = sum(r[0] for r in res)
     wall = max(r[1] for r in res)
     return done / wall, wall
 
 
+def spread(count, sample):
+    """`sample` simulation indices spread evenly over a population of `count`."""
+    sample = min(sample, count)
+    return sorted(set(int(round(x)) for x in np.linspace(0, count - 1, sample)))
+
+
 def _timed_chunk(payload):
-    workload, precision, idx, steps = payload
+    workload, precision, idx, steps, warmup = payload
     import __graft_entry__ as g
     O = g.load_oracle()
     import bridge
@@ -628,21 +661,48 @@ def _timed_chunk(payload):
     models = []
     for i in idx:
         c, p, it = wl.build(i % wl.count)
+        if wl.kind == "stents":
+            p.tolerance_residual = wl.tol_res[i % wl.count]
         models.append(O.OracleModel(bridge.scene_from_conf(c, it), bridge.params_from(p)))
-    t0 = time.perf_counter()
-    done = 0
+    done, busy = 0, 0.0
     for m in models:
-        done += O.run_simulation(m, max_steps=steps)["steps"]
-    return done, time.perf_counter() - t0
+        state = O.run_simulation(m, max_steps=warmup) if warmup else None
+        t0 = time.perf_counter()
+        r = O.run_simulation(m, max_steps=steps, resume=state)
+        busy += time.perf_counter() - t0
+        done += r["steps"] - (state["steps"] if state else 0)
+    return done, busy
 
 
 # ------------------------------------------------------------------ distributed helpers
 
-def dist_init():
+DEVICE = None  # CUDA ordinal this process uses (None: no GPU visible)
+
+
+def device_for_rank(local_rank, n_visible):
+    """The GPU a rank binds: its local rank among the devices it sees.  A launcher that gives each
+    rank one device (CUDA_VISIBLE_DEVICES per rank) leaves one visible device: ordinal 0."""
+    if n_visible < 1:
+        return None
+    return local_rank % n_visible
+
+
+def dist_init(bind=True):
+    """Reads RANK / WORLD_SIZE / LOCAL_RANK, binds this rank's GPU through the library
+    (eb_set_device) whatever CUDA_VISIBLE_DEVICES holds (bind=False: the CPU-only reference
+    arm touches no GPU), and joins the gloo group for the timing barrier and max (N > 1)."""
+    global DEVICE
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    if bind:
+        eb = _pkg()
+        from endobeams_gb300 import _lib
+        n_visible, _ = eb.device_info()
+        DEVICE = device_for_rank(local, n_visible)
+        if DEVICE is not None:
+            _lib.check(_lib.load().eb_set_device(DEVICE), "eb_set_device")
     if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
         import torch.distributed as dist
         dist.init_process_group("gloo")
     return rank, world
@@ -666,28 +726,31 @@ def allreduce_max(x, world):
 
 def main():
     args = parse()
-    rank, world = dist_init()
+    rank, world = dist_init(bind=args.impl != "reference")
     if args.impl == "reference":
         if rank != 0:
             return
         cores = os.cpu_count() or 1
         wl = Workload(args.workload, args.precision, "off", args.count)
-        sample = max(args.cpu_sample, cores)
-        rate, wall = cpu_rate(args.workload, wl.precision, sample, args.cpu_steps, cores)
+        idx = spread(wl.count, args.ref_sample)
+        rate, wall = cpu_rate(args.workload, wl.precision, idx, args.steps, cores, warmup=args.warmup)
+        sample = (f"{len(idx)} of {wl.count} sims spread over the population, {args.warmup} untimed + "
+                  f"{args.steps} timed steps each (the GPU arm's window), C++ oracle + SciPy SuperLU, "
+                  f"{cores} processes, {wall:.1f} s timed")
         line = {"metric": METRIC if wl.kind == "stents" else "HHT steps/s (whole job), batched plain Newton",
                 "impl": "reference", "value": rate, "unit": "HHT steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": {"workload": wl.name, "sims": wl.count},
+                "dtype": "f64", "data": "synthetic", "config": {"workload": wl.name, "sims": wl.count,
+                                                                "sample": len(idx)},
                 "cpu_baseline": {"value": rate, "unit": "HHT steps/s", "cores": cores, "kind": "port",
-                                 "sample": f"{sample} of {wl.count} sims x {args.cpu_steps} steps, "
-                                           f"C++ oracle + SciPy SuperLU, {cores} processes, {wall:.1f} s"},
+                                 "sample": sample},
                 "e2e": {"value": rate, "unit": "HHT steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
     out, wl = gpu_arm(args, rank, world)
     if rank == 0:
         if not args.no_cpu:
-            rate, wall = cpu_rate(args.workload, wl.precision, args.cpu_sample, args.cpu_steps, 1)
+            rate, wall = cpu_rate(args.workload, wl.precision, range(args.cpu_sample), args.cpu_steps, 1)
             out["cpu_baseline"] = {"value": rate, "unit": "HHT steps/s", "cores": 1, "kind": "port",
                                    "sample": f"{args.cpu_sample} of {wl.count} sims x {args.cpu_steps} steps, "
                                              f"C++ oracle + SciPy SuperLU, 1 core, {wall:.1f} s"}

@@ -81,6 +81,9 @@ SIGNATURES = {
     "eb_rollback": (C.c_int, [C.c_void_p, P_i32]),
     "eb_get_state": (C.c_int, [C.c_void_p, C.c_int32] + [P_d] * 8),
     "eb_get_state_n": (C.c_int, [C.c_void_p, C.c_int32] + [P_d] * 8),
+    "eb_set_state": (C.c_int, [C.c_void_p, C.c_int32] + [P_d] * 8),
+    "eb_set_max_iterations": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "eb_set_tolerances": (C.c_int, [C.c_void_p, P_d, P_d]),
     "eb_get_stats": (C.c_int, [C.c_void_p, C.POINTER(EbSimStats)]),
     "eb_get_memory": (C.c_int, [C.c_void_p, P_i64, P_i32]),
     "eb_get_forces": (C.c_int, [C.c_void_p, C.c_int32, P_d, P_d, P_d]),

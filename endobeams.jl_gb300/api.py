@@ -13,7 +13,9 @@ the Julia package reads the same here:
 
 Every step runs on the GPU through libendobeams_gb300 (there is no CPU
 path); ``run_simulations`` runs many independent configurations in one
-batched handle.  VTK output (src/IO/*) is not produced.
+batched handle.  With ``SimulationParams.output_dir`` set, VTK files are
+written as the reference's write_VTK does (src/IO/visualization_beams.jl),
+by the library's asynchronous writer.
 """
 from __future__ import annotations
 
@@ -105,7 +107,7 @@ class ImposedDisplacement:
 
 
 class BoundaryConditions:
-    """BoundaryConditions constructors of def_bcs_and_loads.jl:86-127 (dofs 1-based)."""
+    """BoundaryConditions constructors of def_bcs_and_loads.jl:21-64 (dofs 1-based)."""
 
     def __init__(self, *args):
         ndofs = int(args[-1])
@@ -294,7 +296,7 @@ def read_vtk_sdf(filename: str):
 
 
 class BeamElementSurface:
-    """BeamElementSurface(contact_beams) (def_interactions.jl:172-184); 1-based element ids or a connectivity matrix."""
+    """BeamElementSurface(contact_beams) (def_interactions.jl:52-65); 1-based element ids or a connectivity matrix."""
 
     def __init__(self, x):
         a = np.asarray(x)
@@ -501,6 +503,34 @@ class GpuSimulations:
         check(f(self.h, s, *(ptr(out[k]) for k in ("u", "ud", "udd", "w", "wd", "wdd", "R", "dR"))), "eb_get_state")
         return out
 
+    def set_state(self, s: int, **fields):
+        """Assigns node fields of simulation s between steps (u, ud, udd, w, wd, wdd: n x 3;
+        R, dR: n x 9 column-major), to both its committed and working state (eb_set_state)."""
+        names = ("u", "ud", "udd", "w", "wd", "wdd", "R", "dR")
+        bad = set(fields) - set(names)
+        if bad:
+            raise ValueError(f"unknown node fields {sorted(bad)}")
+        n = len(self.confs[s].nodes)
+        arrs = {k: f64(np.asarray(v, float).reshape(n, 9 if k in ("R", "dR") else 3)) for k, v in fields.items()}
+        check(self.L.eb_set_state(self.h, s, *(ptr(arrs[k]) if k in arrs else None for k in names)), "eb_set_state")
+
+    def set_max_iterations(self, max_iterations=None):
+        """Per-simulation Newton iteration caps (None: params.max_iterations for all)."""
+        if max_iterations is None:
+            check(self.L.eb_set_max_iterations(self.h, None), "eb_set_max_iterations")
+            self.max_iterations = np.full(self.n, int(self.params.max_iterations))
+            return
+        m = i32(np.broadcast_to(np.asarray(max_iterations), (self.n,)))
+        check(self.L.eb_set_max_iterations(self.h, m.ctypes.data_as(C.c_void_p)), "eb_set_max_iterations")
+        self.max_iterations = m.astype(int)
+
+    def set_tolerances(self, residual=None, displacement=None):
+        """Per-simulation Newton tolerances (None: the params value for all simulations)."""
+        r = None if residual is None else f64(np.broadcast_to(np.asarray(residual, float), (self.n,)))
+        d = None if displacement is None else f64(np.broadcast_to(np.asarray(displacement, float), (self.n,)))
+        check(self.L.eb_set_tolerances(self.h, ptr(r) if r is not None else None, ptr(d) if d is not None else None),
+              "eb_set_tolerances")
+
     def forces(self, s: int) -> dict:
         N = 6 * len(self.confs[s].nodes)
         out = {k: np.zeros(N) for k in ("Tint", "Tk", "Tc")}
@@ -651,6 +681,9 @@ class RunResult:
     wall_s: float
     newton_iterations: List[int] = field(default_factory=list)
     krylov_iterations: List[int] = field(default_factory=list)
+    # per simulation: True when its Δt fell below min_timestep and it stopped at its last
+    # converged state (the reference aborts that simulation, run_simulation.jl:61-66)
+    aborted: List[bool] = field(default_factory=list)
 
 
 def output_dirs(output_dir: str, n: int) -> List[str]:
@@ -663,14 +696,22 @@ def output_dirs(output_dir: str, n: int) -> List[str]:
 
 def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Optional[int] = None,
                     engine: Optional[GpuSimulations] = None, on_step=None, points_per_beam: int = 10) -> RunResult:
-    """The time loop of run_simulation! (run_simulation.jl:170-244) for many
+    """The time loop of run_simulation! (run_simulation.jl:38-112) for many
     configurations at once: each keeps its own t, Δt and success counter, and
     all simulations still running advance together in one batched step.
 
     With params.output_dir set, VTK files are written as the reference does
     (run_simulation.jl:30-32, 86-90: the initial state, then after a converged
     step once output_timestep has passed, labelled with the step's start time),
-    by the library's asynchronous writer (one directory per simulation)."""
+    by the library's asynchronous writer (one directory per simulation).
+
+    A simulation whose halved Δt falls below min_timestep is aborted on its
+    own (the reference raises "Simulation aborted." for its one simulation,
+    run_simulation.jl:61-66): it is rolled back to its last converged state and
+    leaves the batch, the others run on unchanged, and ``RunResult.aborted``
+    marks it.  A step whose norms are not finite (EB_SIM_NAN) counts as not
+    converged, so it is rolled back and retried with half the Δt like any
+    other failed step."""
     eng = engine or GpuSimulations(confs, params, inters)
     p = params
     S = eng.n
@@ -681,6 +722,7 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
     ks = [[] for _ in range(S)]
     newton = np.zeros(S, int)
     krylov = np.zeros(S, int)
+    aborted = np.zeros(S, bool)
     tuned = False
     out = bool(p.output_dir)
     if out:
@@ -691,7 +733,7 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
         counter += 1
     t0 = time.perf_counter()
     while True:
-        running = (p.simulation_end_time - t > 1.0e-10)
+        running = (p.simulation_end_time - t > 1.0e-10) & ~aborted
         if max_steps is not None:
             running &= step <= max_steps
         if not running.any():
@@ -704,16 +746,17 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
         for s in np.nonzero(running)[0]:
             newton[s] += st[s]["newton_iterations"]
             krylov[s] += st[s]["krylov_iterations"]
-        failed = running & (k > p.max_iterations)       # run_simulation.jl:187-203
+        maxit = getattr(eng, "max_iterations", None)
+        maxit = np.full(S, p.max_iterations) if maxit is None else np.asarray(maxit)
+        failed = running & (k > maxit)                  # run_simulation.jl:55-71
         ok = running & ~failed
         if failed.any():
             dt[failed] = dt[failed] / 2
-            if (dt[failed] < p.min_timestep).any():
-                raise RuntimeError("Simulation aborted: Δt < min_timestep")
-            eng.rollback(failed.astype(np.int32))
+            aborted |= failed & (dt < p.min_timestep)     # :61-66, per simulation
+            eng.rollback(failed.astype(np.int32))        # update_not_converged!, :69
             succ[failed] = 0
         succ[ok] += 1
-        grow = ok & (succ >= p.accelerate_after_success_it) & (k <= 8)  # :211-216
+        grow = ok & (succ >= p.accelerate_after_success_it) & (k <= 8)  # :79-84
         dt[grow] = np.minimum(dt[grow] * 1.5, p.max_timestep)
         succ[grow] = 0
         if out:
@@ -726,7 +769,7 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
                 counter[w] += 1
                 write_t[w] = t1[w]
         if ok.any():
-            eng.commit(ok.astype(np.int32))              # update_converged!, :232
+            eng.commit(ok.astype(np.int32))              # update_converged!, :100
         for s in np.nonzero(ok)[0]:
             ks[s].append(int(k[s]))
         t[ok] = t[ok] + dt_used[ok]
@@ -741,10 +784,16 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
     wall = time.perf_counter() - t0
     eng.sync_nodes()
     return RunResult(steps=list(step - 1), ks=ks, t=list(t), wall_s=wall, newton_iterations=list(newton),
-                     krylov_iterations=list(krylov))
+                     krylov_iterations=list(krylov), aborted=[bool(a) for a in aborted])
 
 
 def run_simulation(conf: BeamsConfiguration, params: SimulationParams, inter: Optional[RigidInteraction] = None,
                    max_steps: Optional[int] = None) -> RunResult:
-    """run_simulation!(conf, params, inter) (src/run_simulation.jl:133-251) on the GPU."""
-    return run_simulations([conf], params, [inter], max_steps=max_steps)
+    """run_simulation!(conf, params, inter) (src/run_simulation.jl:1-119) on the GPU.
+
+    Like the reference, raises when Δt falls below min_timestep (run_simulation.jl:61-66); the
+    configuration's nodes then hold the last converged state."""
+    res = run_simulations([conf], params, [inter], max_steps=max_steps)
+    if res.aborted[0]:
+        raise RuntimeError("Simulation aborted: Δt < min_timestep")
+    return res

@@ -67,7 +67,7 @@ struct Arena {
 
 // ---------------------------------------------------------------- geometry helpers (host, FP64)
 
-// get_Rₑ⁰ (src/beams/def_beam.jl:163-186), column-major output
+// get_Rₑ⁰ (src/beams/def_beam.jl:93-116), column-major output
 void initial_frame(const double* X1, const double* X2, double* R) {
   const double eps = 2.220446049250313e-16;
   double d[3] = {X2[0] - X1[0], X2[1] - X1[1], X2[2] - X1[2]};
@@ -386,6 +386,8 @@ struct eb_handle {
   double* d_relres = nullptr;
   std::vector<eb_sim_stats> stats;
   std::vector<double> h_norms;
+  std::vector<int> max_it;  // per simulation Newton iteration cap (params.max_iterations unless set)
+  std::vector<double> tol_res, tol_disp;  // per simulation Newton tolerances (params unless set)
   // band-LU preconditioner
   bool any_band = false, any_jacobi = false;
   int max_b = 0;
@@ -757,7 +759,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
       if (S.Re0) std::memcpy(Rm, S.Re0 + 9 * e, sizeof(Rm));
       else initial_frame(Xa, Xb, Rm);
       for (int k = 0; k < 9; ++k) Re0[k * NE + ge] = Rm[k];
-      // BeamMaterialProperties / K̄ⁱⁿᵗ_beam (def_beam.jl:144-155, 205-219)
+      // BeamMaterialProperties / K̄ⁱⁿᵗ_beam (def_beam.jl:74-85, 135-149)
       const double E = S.E[e], nu = S.nu[e], rho = S.rho[e], r = S.radius[e];
       const double G = E / (2 * (1 + nu));
       const double A = M_PI * r * r;
@@ -814,7 +816,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     has_fixed[s] = S.n_fixed > 0;
     for (int64_t k = 0; k < S.n_loaded; ++k) {
       h->load_dof.push_back(6 * no + S.loaded_dofs[k]);
-      fext[6 * no + S.loaded_dofs[k]] = S.fext0 ? S.fext0[k] : 0.0;  // Forces(conf), def_structures.jl:155-167
+      fext[6 * no + S.loaded_dofs[k]] = S.fext0 ? S.fext0[k] : 0.0;  // Forces(conf), def_structures.jl:10-31
     }
     h->fix_off[s + 1] = h->fix_off[s] + S.n_fixed;
     h->load_off[s + 1] = h->load_off[s] + S.n_loaded;
@@ -1074,6 +1076,9 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   CK(A.alloc(&sa.prev_eta, n_sims));
   h->stats.assign(n_sims, eb_sim_stats{});
   h->h_norms.assign(5 * (size_t)n_sims, 0.0);
+  h->max_it.assign(n_sims, p->max_iterations);
+  h->tol_res.assign(n_sims, p->tolerance_residual);
+  h->tol_disp.assign(n_sims, p->tolerance_displacement);
 
   // ---- band storage (falls back to block-Jacobi when it would not fit in half the free memory)
   {
@@ -1584,7 +1589,8 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
   if (h->sa.forcing) CK(cudaMemsetAsync(h->sa.prev_bnorm, 0, sizeof(double) * S, st));  // first corrector solve: forcing_max
   std::vector<double> res(S, INFINITY), dn(S, INFINITY);
   std::vector<int> running(S);
-  for (int s = 0; s < S; ++s) running[s] = act[s] && (1 <= P.max_iterations);
+  const std::vector<int>& max_it = h->max_it;
+  for (int s = 0; s < S; ++s) running[s] = act[s] && (1 <= max_it[s]);
   bool first = true;
   std::fill(ws.used.begin(), ws.used.end(), 0);
   while (true) {
@@ -1646,7 +1652,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
         disable_staging(h);
         h->graph_gen += 1;
         running[s] = 0;
-        k[s] = P.max_iterations + 1;
+        k[s] = max_it[s] + 1;
         continue;
       }
       if (h->P.refactor_its > 0 && q[4] > h->P.refactor_its) h->need_refactor[s] = 1;
@@ -1659,7 +1665,15 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
       dn[s] = dnorm;
       ++iter[s];
       k[s] += 1;
-      running[s] = (res[s] > P.tolerance_residual || dn[s] > P.tolerance_displacement) && k[s] <= P.max_iterations;
+      if (!std::isfinite(rn) || !std::isfinite(dnorm)) {
+        // The reference's loop test (corrector.jl:15) is false for NaN norms, so it would
+        // accept the step; here the simulation stops iterating and the step is reported not
+        // converged (EB_SIM_NAN), so its caller rolls it back instead of committing NaNs.
+        running[s] = 0;
+        k[s] = max_it[s] + 1;
+        continue;
+      }
+      running[s] = (res[s] > h->tol_res[s] || dn[s] > h->tol_disp[s]) && k[s] <= max_it[s];
     }
   }
   // ---- statistics
@@ -1675,11 +1689,11 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     if (!act[s]) continue;
     int stt = status[s];
     if (stt != EB_SIM_WAIT_TIMEOUT && (!std::isfinite(res[s]) || !std::isfinite(dn[s]))) stt = EB_SIM_NAN;
-    if (k[s] > P.max_iterations && stt == EB_SIM_OK) stt = EB_SIM_NOT_CONVERGED;
+    if (k[s] > max_it[s] && stt == EB_SIM_OK) stt = EB_SIM_NOT_CONVERGED;
     if (stt == EB_SIM_WAIT_TIMEOUT) {
       // the step's solves are not trusted: report "not converged" (the caller rolls back)
       // and read band blocks from global memory from now on
-      k[s] = P.max_iterations + 1;
+      k[s] = max_it[s] + 1;
       disable_staging(h);
       h->graph_gen += 1;
     }
@@ -1750,6 +1764,55 @@ int eb_get_state(eb_handle* h, int32_t sim, double* u, double* ud, double* udd, 
 int eb_get_state_n(eb_handle* h, int32_t sim, double* u, double* ud, double* udd, double* w, double* wd,
                    double* wdd, double* R, double* dR) {
   return get_state_impl(h, sim, true, u, ud, udd, w, wd, wdd, R, dR);
+}
+
+// Writes one simulation's node record into both the committed state (n) and the working
+// state (n+1); fields passed as NULL are left as they are.
+int eb_set_state(eb_handle* h, int32_t sim, const double* u, const double* ud, const double* udd, const double* w,
+                 const double* wd, const double* wdd, const double* R, const double* dR) {
+  if (!h || sim < 0 || sim >= h->n_sims) return fail(EB_ERR_ARG, "eb_set_state: bad handle or sim index");
+  if (h->mid_step) return fail(EB_ERR_STATE, "eb_set_state: between eb_step and eb_commit/eb_rollback");
+  const int64_t NN = h->d.n_nodes, o = h->node_off[sim], n = h->node_off[sim + 1] - o;
+  const Dev& d = h->d;
+  double* dst[8][2] = {{d.u, d.un},   {d.ud, d.udn}, {d.udd, d.uddn}, {d.w, d.wn},
+                       {d.wd, d.wdn}, {d.wdd, d.wddn}, {d.R, d.Rn},   {d.dR, d.dRn}};
+  const double* src[8] = {u, ud, udd, w, wd, wdd, R, dR};
+  const int nc[8] = {3, 3, 3, 3, 3, 3, 9, 9};
+  std::vector<double> tmp((size_t)n);
+  CK(cudaStreamSynchronize(h->stream));
+  for (int f = 0; f < 8; ++f) {
+    if (!src[f]) continue;
+    for (int k = 0; k < nc[f]; ++k) {
+      for (int64_t i = 0; i < n; ++i) tmp[i] = src[f][nc[f] * i + k];
+      for (int t = 0; t < 2; ++t)
+        CK(cudaMemcpy(dst[f][t] + k * NN + o, tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    }
+  }
+  return EB_OK;
+}
+
+int eb_set_max_iterations(eb_handle* h, const int32_t* max_iterations) {
+  if (!h) return fail(EB_ERR_ARG, "eb_set_max_iterations: null handle");
+  for (int s = 0; s < h->n_sims; ++s) {
+    const int m = max_iterations ? max_iterations[s] : h->P.max_iterations;
+    if (m < 0) return fail(EB_ERR_ARG, "eb_set_max_iterations: negative cap for simulation %d", s);
+  }
+  for (int s = 0; s < h->n_sims; ++s) h->max_it[s] = max_iterations ? max_iterations[s] : h->P.max_iterations;
+  return EB_OK;
+}
+
+int eb_set_tolerances(eb_handle* h, const double* tolerance_residual, const double* tolerance_displacement) {
+  if (!h) return fail(EB_ERR_ARG, "eb_set_tolerances: null handle");
+  for (int s = 0; s < h->n_sims; ++s) {
+    const double r = tolerance_residual ? tolerance_residual[s] : h->P.tolerance_residual;
+    const double d = tolerance_displacement ? tolerance_displacement[s] : h->P.tolerance_displacement;
+    if (!(r >= 0) || !(d >= 0)) return fail(EB_ERR_ARG, "eb_set_tolerances: bad tolerance for simulation %d", s);
+  }
+  for (int s = 0; s < h->n_sims; ++s) {
+    h->tol_res[s] = tolerance_residual ? tolerance_residual[s] : h->P.tolerance_residual;
+    h->tol_disp[s] = tolerance_displacement ? tolerance_displacement[s] : h->P.tolerance_displacement;
+  }
+  return EB_OK;
 }
 
 int eb_get_stats(eb_handle* h, eb_sim_stats* stats) {

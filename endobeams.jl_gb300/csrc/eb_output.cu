@@ -429,6 +429,14 @@ int vtk_write(VtkWriter* w, const int32_t* mask, const int32_t* counter, const i
     }
     cudaError_t e = cudaSuccess;
     if (sl.copied_recorded) e = cudaStreamWaitEvent(w->stream, sl.copied, 0);
+    if (e != cudaSuccess) {
+      // without the wait the kernels could overwrite the slot while its previous copy still
+      // reads it: return before launching anything into the slot
+      std::lock_guard<std::mutex> lk(w->mu);
+      sl.busy = false;
+      err = std::string("vtk_write: ") + cudaGetErrorString(e);
+      return -1;
+    }
     const int64_t nb = beam_output_doubles(S.ne, w->pts);
     launch_beam_output(w->d, w->E, S.e0, S.ne, w->pts, sl.dev, w->stream);
     launch_node_output(w->d, S.n0, S.nn, sl.dev + nb, w->stream);

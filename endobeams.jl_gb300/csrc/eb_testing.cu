@@ -8,6 +8,7 @@
 // K̄ΘΘ[3] Jᵨ[3] Aᵨ damping radius (pad).  3x3 matrices column-major.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -143,16 +144,38 @@ extern "C" int eb_contact_eval(int64_t n, const double* in, const double* gauss6
 
 // ---------------------------------------------------------------- contact evaluation without allocation
 // Variant of eb_contact_eval for callers that cannot allocate device memory
-// during the call (inside stream capture, or under a caller-owned memory
-// pool): the caller's device buffers are used directly, and the prefiltered
-// SDF coefficients go to the fixed array below instead of a cudaMalloc.
+// during the call (a host whose device memory belongs to its own pool
+// allocator, a loop that forbids allocation after start-up): the caller's
+// device buffers are used directly, and the prefiltered SDF coefficients go
+// to the fixed array below instead of a cudaMalloc.
 namespace {
 
 __device__ __align__(256) double g_noalloc_coef[EB_NOALLOC_SDF_MAX_COEFS];
 
 std::mutex g_noalloc_mu;
 constexpr int kMaxDevices = 64;
-double* g_noalloc_ptr[kMaxDevices] = {nullptr};  // device address of g_noalloc_coef, per device ordinal
+// Device address of g_noalloc_coef per device ordinal, and the context it was looked up in:
+// after cudaDeviceReset (or any other re-creation of the device's context) the address is
+// looked up again.
+double* g_noalloc_ptr[kMaxDevices] = {nullptr};
+void* g_noalloc_ctx[kMaxDevices] = {nullptr};
+
+// The calling thread's current driver context (an opaque handle), through the runtime's
+// driver entry-point query so the library does not link the driver API; nullptr if unknown.
+void* current_context() {
+  using GetCurrent = int (*)(void**);
+  static GetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return (GetCurrent)f;
+  }();
+  void* ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
 
 __global__ void k_sdf_interior(const double* __restrict__ vals, int nx, int ny, int nz, double* __restrict__ c) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -226,6 +249,11 @@ extern "C" int eb_contact_eval_noalloc(int64_t n, const double* d_in, const doub
   Gauss3 g;
   for (int i = 0; i < 3; ++i) { g.w[i] = gauss6[i]; g.z[i] = gauss6[3 + i]; }
   ContactProps cp{props[0], props[1], props[2], props[3]};
+  // surface kind (0 sphere, 1 SDF, 2 plane) and the plane's axis are whole numbers in range
+  // before they are converted
+  if (!(surf[0] == 0 || surf[0] == 1 || surf[0] == 2) ||
+      (surf[0] == 2 && !(surf[1] == 0 || surf[1] == 1 || surf[1] == 2)))
+    return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad surface kind or plane axis");
   SurfaceDev s;
   std::memset(&s, 0, sizeof(s));
   s.kind = (int)surf[0];
@@ -234,14 +262,21 @@ extern "C" int eb_contact_eval_noalloc(int64_t n, const double* d_in, const doub
     s.axis = (int)surf[1];
     s.pos = surf[2];
   }
-  if (s.kind < 0 || s.kind > 2 || s.axis < 0 || s.axis > 2)
-    return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad surface kind or plane axis");
   if (s.kind == 1) {
-    const int64_t nx = (int64_t)surf[5], ny = (int64_t)surf[6], nz = (int64_t)surf[7];
     if (!d_sdf_values) return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: SDF values missing");
-    if (nx < 1 || ny < 1 || nz < 1 || !(surf[11] > 0) || !(surf[12] > 0) || !(surf[13] > 0))
-      return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad SDF grid");
-    if ((nx + 2) * (ny + 2) * (nz + 2) > (int64_t)EB_NOALLOC_SDF_MAX_COEFS)
+    // every grid dimension is checked on its own (finite, at least 1, within the array) before
+    // the padded product is formed, so the product cannot overflow
+    const double lim = (double)EB_NOALLOC_SDF_MAX_COEFS;
+    for (int a = 5; a < 8; ++a)
+      if (!std::isfinite(surf[a]) || !(surf[a] >= 1) || !(surf[a] <= lim) || surf[a] != std::floor(surf[a]))
+        return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad SDF grid dimension (surf[5..7] must be "
+                                            "integers in [1, EB_NOALLOC_SDF_MAX_COEFS])");
+    for (int a = 8; a < 14; ++a)
+      if (!std::isfinite(surf[a]) || (a >= 11 && !(surf[a] > 0)))
+        return eb_internal_fail(EB_ERR_ARG, "eb_contact_eval_noalloc: bad SDF origin or spacing (surf[8..13])");
+    const int64_t nx = (int64_t)surf[5], ny = (int64_t)surf[6], nz = (int64_t)surf[7];
+    if ((nx + 2) > (int64_t)EB_NOALLOC_SDF_MAX_COEFS / ((ny + 2) * (nz + 2)) ||
+        (nx + 2) * (ny + 2) * (nz + 2) > (int64_t)EB_NOALLOC_SDF_MAX_COEFS)
       return eb_internal_fail(EB_ERR_ARG,
                               "eb_contact_eval_noalloc: SDF grid too large for the fixed coefficient array "
                               "((nx+2)(ny+2)(nz+2) > EB_NOALLOC_SDF_MAX_COEFS = 287496)");
@@ -252,11 +287,13 @@ extern "C" int eb_contact_eval_noalloc(int64_t n, const double* d_in, const doub
     double* coef = nullptr;
     {
       std::lock_guard<std::mutex> lk(g_noalloc_mu);
-      if (!g_noalloc_ptr[dev]) {
+      void* ctx = current_context();
+      if (!g_noalloc_ptr[dev] || !ctx || ctx != g_noalloc_ctx[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_coef);
         if (e != cudaSuccess) return err("cudaGetSymbolAddress", e);
         g_noalloc_ptr[dev] = (double*)p;
+        g_noalloc_ctx[dev] = current_context();
       }
       coef = g_noalloc_ptr[dev];
     }

@@ -10,6 +10,10 @@ Each builder returns ``(conf, params, inter)`` built with the public API:
 * ``net_on_sphere``     — one jittered square net dropped on a sphere SDF (configuration 2, one sim).
 * ``braided_stent``     — braided stent with merged crossings released in a cylinder SDF
   (configurations 3 and 4).
+* ``reference_net_on_sphere`` — the net of the reference's contact test
+  (test/test_beams2rigid_contact_1_analytical.jl:14-107) on its analytic sphere.
+* ``reference_imposed_wave``  — the reference's beam driven by an imposed triangular wave
+  against an analytic sphere (test/test_beams2rigid_contact_2_analytical.jl:13-128).
 
 Gravity is not implemented in the reference (def_bcs_and_loads.jl:80); it is
 applied here as constant nodal `ConcentratedForce`s: f_z = -g ρA Σ l/2 over
@@ -23,8 +27,8 @@ from typing import Optional
 import numpy as np
 
 from .api import (BeamElementSurface, Beams, BeamsConfiguration, BoundaryConditions, ConcentratedForce,
-                  DiscreteSignedDistanceField, Encastre, InteractionProperties, Loads, NodesBeams,
-                  PlaneSurface, RigidInteraction, SimulationParams, SphereSurface)
+                  DiscreteSignedDistanceField, Encastre, ImposedDisplacement, InteractionProperties, Loads,
+                  NodesBeams, PlaneSurface, RigidInteraction, SimulationParams, SphereSurface)
 
 G_ACC = 9.81
 
@@ -263,3 +267,57 @@ def stent_variant(v: dict, steps: int = 10000, tol: float = 1e-8, precision: str
     return braided_stent(wires=v["wires"], R=v["R"], pitch_deg=v["pitch_deg"], elems_per_wire=v["elems_per_wire"],
                          crossing_every=None, length=length, cyl_radius=v["cyl_frac"] * v["R"], grid=None,
                          steps=steps, tol=tol, precision=precision)
+
+
+# ------------------------------------------------------------------ the reference's own contact scenes
+
+def reference_net_on_sphere(positions, connectivity, steps: Optional[int] = None, end_time: float = 100.0):
+    """test/test_beams2rigid_contact_1_analytical.jl:14-107: a net (node positions and 1-based
+    connectivity as the test reads them from test/input/pos_net.txt and conn_net.txt) moving at
+    u̇_y = -1 mm/s onto a sphere R = 55 mm at the origin; E = 10 Pa, ν = 0, ρ = 1500, r = 0.2 mm,
+    damping 1e-3; kₙ = 1e-6, μ = 0.01, εᵗ = 0.5, ηₙ = 1e-3; α = -0.2, Δt from 0.01 (min 1e-6,
+    max 0.1), tolerances 1e-3.  ``steps`` limits the run (the reference runs to t = 100 s)."""
+    X = np.asarray(positions, float)
+    conn = np.asarray(connectivity, np.int64)
+    ud0 = np.zeros_like(X)
+    ud0[:, 1] = -0.001
+    nodes = NodesBeams(X, None, ud0, None, None, None, None, plane="xy")
+    beams = Beams(nodes, conn, 10.0, 0.0, 1500.0, 2e-4, 1e-3)
+    conf = BeamsConfiguration(nodes, beams, None, None)
+    inter = RigidInteraction(SphereSurface([0.0, 0.0, 0.0], 0.055), BeamElementSurface(conn),
+                             InteractionProperties(1e-6, 0.01, 0.5, 1e-3, 1e-6, 1e-3, 0.0))
+    params = SimulationParams(**hht(-0.2), initial_timestep=0.01, min_timestep=1e-6, max_timestep=0.1,
+                              output_timestep=1.0, simulation_end_time=end_time, tolerance_residual=1e-3,
+                              tolerance_displacement=1e-3, max_iterations=20)
+    return conf, params, inter
+
+
+def wave_displacement(t: float, max_displacement: float = 0.1, time_threshold: float = 2.5) -> float:
+    """The imposed x-displacement of test_beams2rigid_contact_2_analytical.jl:64-73: a triangular
+    wave of amplitude 10 cm and quarter period 2.5 s (zero after 4 quarters)."""
+    v = max_displacement / time_threshold
+    T = time_threshold
+    return ((t <= T) * v * t + (T < t <= 2 * T) * (-v * t + 2 * max_displacement)
+            + (2 * T < t <= 3 * T) * v * (t - 2 * T) + (3 * T < t <= 4 * T) * (-v * t + 4 * max_displacement))
+
+
+def reference_imposed_wave(end_time: float = 2.5):
+    """test/test_beams2rigid_contact_2_analytical.jl:13-128: a 10 cm beam along z (20
+    elements), node 1's DOFs 2:6 clamped and DOF 1 (u_x) driven by ``wave_displacement``,
+    pushed against a sphere R = 4 cm centred at (5, 0.5, 8) cm; E = 50 MPa, ν = 0.33,
+    ρ = 7850, r = 0.3 mm; kₙ = 10, μ = 0, εᵗ = 100, ηₙ = 1e-3; α = -0.05, Δt = 0.01
+    (min 1e-6), tolerances 1e-5, at most 5 Newton iterations."""
+    L, n = 0.1, 20
+    X = np.zeros((n + 1, 3))
+    X[:, 2] = np.linspace(0.0, L, n + 1)
+    nodes = NodesBeams(X, plane="xy")
+    conn = np.array([[i + 1, i + 2] for i in range(n)])
+    beams = Beams(nodes, conn, 5e7, 0.33, 7850.0, 3e-4, 0.0)
+    bcs = BoundaryConditions(Encastre(range(2, 7)), ImposedDisplacement(1, wave_displacement), 6 * (n + 1))
+    conf = BeamsConfiguration(nodes, beams, None, bcs)
+    inter = RigidInteraction(SphereSurface([0.05, 0.005, 0.08], 0.04), BeamElementSurface(conn),
+                             InteractionProperties(10.0, 0.0, 100.0, 1e-3, 10.0, 1e-3, 0.0))
+    params = SimulationParams(**hht(-0.05), initial_timestep=1e-2, min_timestep=1e-6, max_timestep=1e-2,
+                              output_timestep=1e-2, simulation_end_time=end_time, tolerance_residual=1e-5,
+                              tolerance_displacement=1e-5, max_iterations=5)
+    return conf, params, inter

@@ -194,6 +194,21 @@ int eb_get_state(eb_handle *h, int32_t sim, double *u, double *ud, double *udd, 
 /* Node state at n (the last converged step). */
 int eb_get_state_n(eb_handle *h, int32_t sim, double *u, double *ud, double *udd, double *w, double *wd,
                    double *wdd, double *R, double *dR);
+/* Assigns one simulation's NodeBeam fields between steps (src/beams/def_node_beam.jl:6-48: the
+ * reference's nodes are plain mutable records a script may change between steps): written
+ * to both the committed state n and the working state n+1; NULL fields are left unchanged.
+ * Layout as eb_get_state (n x 3, R and ΔR n x 9 column-major).  EB_ERR_STATE between eb_step
+ * and eb_commit/eb_rollback. */
+int eb_set_state(eb_handle *h, int32_t sim, const double *u, const double *ud, const double *udd, const double *w,
+                 const double *wd, const double *wdd, const double *R, const double *dR);
+/* Newton iteration cap per simulation (n_sims values; NULL: params.max_iterations for all).
+ * The reference keeps max_iterations in each simulation's own SimulationParams
+ * (src/def_params.jl:1-35, corrector.jl:15); a batch of simulations may differ in it. */
+int eb_set_max_iterations(eb_handle *h, const int32_t *max_iterations);
+/* Newton tolerances per simulation (n_sims values each; NULL: the params value for all) —
+ * tolerance_residual / tolerance_displacement of each simulation's own SimulationParams
+ * (src/def_params.jl:1-35), tested as in corrector.jl:15. */
+int eb_set_tolerances(eb_handle *h, const double *tolerance_residual, const double *tolerance_displacement);
 int eb_get_stats(eb_handle *h, eb_sim_stats *stats /* n_sims */);
 /* Device memory the handle holds (bytes), and how many simulations use the band-LU preconditioner. */
 int eb_get_memory(eb_handle *h, int64_t *device_bytes, int32_t *band_sims);
@@ -256,20 +271,24 @@ int eb_contact_eval(int64_t n, const double *in, const double *gauss6, const dou
 
 /* Contact evaluation that allocates no memory.  No counterpart in the
  * reference: it exists for callers that must not allocate device memory
- * during a call — code running inside CUDA stream capture (where cudaMalloc
- * is not allowed), hosts whose device memory is owned by their own pool
- * allocator (a Julia or PyTorch runtime), and real-time loops that forbid
- * allocation after start-up.  Same arithmetic and outputs as
+ * during a call — hosts whose device memory is owned by their own pool
+ * allocator (a Julia or PyTorch runtime that has reserved most of the GPU,
+ * where a cudaMalloc behind its back fails or fragments its pool), and
+ * real-time loops that forbid allocation after start-up.  Same arithmetic
+ * and outputs as
  * eb_contact_eval, but every pointer named d_* is DEVICE memory supplied by
  * the caller (n x 96 inputs, the SDF grid, n x 301 outputs, n flags);
  * gauss6, props and surf are small host arrays as in eb_contact_eval.
  * The prefiltered SDF coefficients live in one fixed device array of
  * EB_NOALLOC_SDF_MAX_COEFS doubles (2.3 MB, held on every GPU that loads
  * the library until the process exits): grids with (nx+2)(ny+2)(nz+2)
- * above that (64^3 points) are rejected with EB_ERR_ARG.  The first call on
- * a device looks up that array's device address; make that first call
- * before any stream capture.  All calls share the array: calls that
- * overlap on the GPU (different streams, or different host threads) race.
+ * above that (64^3 points), and grid dimensions that are not whole numbers
+ * in range, are rejected with EB_ERR_ARG before anything is launched.  The
+ * first call on a device (and the first after its context is re-created,
+ * e.g. by cudaDeviceReset) looks up that array's device address; make that
+ * first call before any stream capture.  All calls share the array and each
+ * overwrites it: calls that overlap on the GPU (different streams, or
+ * different host threads) race.
  * stream may be NULL (legacy default stream); the call is asynchronous. */
 #define EB_NOALLOC_SDF_MAX_COEFS 287496
 int eb_contact_eval_noalloc(int64_t n, const double *d_in, const double *gauss6, const double *props,

@@ -2,7 +2,7 @@
 //
 // Small fixed-size FP64 linear algebra used by the CPU restatement of the
 // EndoBeams.jl hot path.  Storage is column-major like Julia's StaticArrays
-// (`Mat33` of src/beams/utils_beams.jl:251), so `m(i,j)` is `a[i + 3*j]`.
+// (`Mat33` of src/constants.jl:1), so `m(i,j)` is `a[i + 3*j]`.
 // Every operation is the plain textbook formula, evaluated left to right,
 // without fused multiply-add (the build passes -ffp-contract=off), so the
 // oracle gives the same bits on x86-64 and aarch64 hosts.

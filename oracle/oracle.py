@@ -10,10 +10,10 @@ The element, contact and nodal-rotation arithmetic runs in the C++ library
 headers); this file restates the step algebra of the reference:
 
 * sparsity pattern and 144-entry scatter maps — src/sparse_matrices.jl:6-104
-* material constants and Rₑ⁰ — src/beams/def_beam.jl:144-219
+* material constants and Rₑ⁰ — src/beams/def_beam.jl:74-149
 * predictor / corrector / step — src/predictor.jl, src/corrector.jl,
   src/solve_step_dynamics.jl, src/utils_solver.jl, src/utils_bcs_and_loads.jl
-* time loop and Δt policy — src/run_simulation.jl:170-244
+* time loop and Δt policy — src/run_simulation.jl:38-112
 
 The linear solve of src/linearsolvers.jl (MKL PARDISO, closed binary, not
 present) is replaced by SciPy's SuperLU, an exact sparse LU like PARDISO.
@@ -117,7 +117,7 @@ def sdf_eval_batch(surf: np.ndarray, coef: np.ndarray, pts: np.ndarray, radius: 
 # ----------------------------------------------------------------- model setup
 
 def beam_constants(E, nu, rho, radius, l0):
-    """BeamMaterialProperties + K̄ⁱⁿᵗ_beam (def_beam.jl:144-155, 205-219).
+    """BeamMaterialProperties + K̄ⁱⁿᵗ_beam (def_beam.jl:74-85, 135-149).
 
     Returns Kbar (n,7) = [K̄ū, K̄Θ(3), K̄ΘΘ(3)], Jr (n,3), Ar (n,)."""
     E, nu, rho, radius, l0 = (np.broadcast_to(np.asarray(x, float), np.shape(l0)) for x in (E, nu, rho, radius, l0))
@@ -134,7 +134,7 @@ def beam_constants(E, nu, rho, radius, l0):
 
 
 def get_Re0(X1: np.ndarray, X2: np.ndarray) -> np.ndarray:
-    """get_Rₑ⁰ (def_beam.jl:163-186); returns (n,9) column-major."""
+    """get_Rₑ⁰ (def_beam.jl:93-116); returns (n,9) column-major."""
     out = np.zeros((X1.shape[0], 9))
     for e in range(X1.shape[0]):
         d = X2[e] - X1[e]
@@ -482,18 +482,22 @@ class OracleModel:
                     wdd=self.wdd.copy(), R=self.R.copy(), dR=self.dR.copy())
 
 
-def run_simulation(model: OracleModel, max_steps: Optional[int] = None, on_step=None):
-    """run_simulation! time loop (run_simulation.jl:170-244), without file output.
+def run_simulation(model: OracleModel, max_steps: Optional[int] = None, on_step=None, resume: Optional[dict] = None):
+    """run_simulation! time loop (run_simulation.jl:38-112), without file output.
 
-    Returns a dict with the step count, the per-step k values and the final time."""
+    Returns a dict with the step count, the per-step k values and the final time.
+    ``resume`` (a dict returned by an earlier call on the same model, or None) continues that
+    loop where it stopped — its t, Δt, success counter and step number — for ``max_steps``
+    more committed steps."""
     p = model.p
-    t = 0.0
-    dt = p.initial_timestep
-    succ = 0
-    step = 1
+    t = resume["t"] if resume else 0.0
+    dt = resume["dt"] if resume else p.initial_timestep
+    succ = resume["succ"] if resume else 0
+    step0 = resume["steps"] if resume else 0
+    step = step0 + 1
     ks = []
     while p.simulation_end_time - t > 1.0e-10:
-        if max_steps is not None and step > max_steps:
+        if max_steps is not None and step > step0 + max_steps:
             break
         t1 = t + dt
         n_it = model.step(t1, dt)
@@ -514,4 +518,4 @@ def run_simulation(model: OracleModel, max_steps: Optional[int] = None, on_step=
             on_step(step, t1, dt, n_it)
         t = t1
         step += 1
-    return dict(steps=step - 1, ks=ks, t=t, dt=dt)
+    return dict(steps=step - 1, ks=ks, t=t, dt=dt, succ=succ)

@@ -1,6 +1,6 @@
 """Host-side logic that needs no GPU: API semantics, scene generators, and the
 batched time loop's Δt policy against the oracle's restatement of
-run_simulation.jl:170-244 on scripted Newton outcomes."""
+run_simulation.jl:38-112 on scripted Newton outcomes."""
 import numpy as np
 import pytest
 
@@ -206,3 +206,36 @@ def test_triangulated_surface_grid_covers_the_mesh(eb):
     assert np.all(hi >= V.max(0) + 2 * h - 1e-12)
     ts2 = eb.TriangulatedSurface(V, T)  # default spacing: 1/64 of the largest extent
     assert ts2.grid()[1] == pytest.approx(2.0 / 64)
+
+
+def test_one_simulation_aborts_alone(eb):
+    """A simulation whose Δt falls below min_timestep leaves the batch on its own (the reference
+    aborts its one simulation, run_simulation.jl:61-66): it is rolled back at every failure and
+    never committed again, while the other simulation takes exactly the steps it takes alone."""
+    p = eb.SimulationParams(alpha=-0.05, beta=0.28, gamma=0.55, initial_timestep=0.01, min_timestep=1e-3,
+                            max_timestep=0.02, simulation_end_time=0.1, max_iterations=20)
+    good = [3] * 80
+    bad = [3, 3] + [21] * 80                     # converges twice, then never again
+    alone = _ScriptedEngine([list(good)])
+    ra = eb.run_simulations([None], p, engine=alone)
+    eng = _ScriptedEngine([list(bad), list(good)])
+    res = eb.run_simulations([None, None], p, engine=eng)
+    assert res.aborted == [True, False]
+    assert res.steps[0] == 2 and res.ks[0] == [3, 3]
+    assert res.steps[1] == ra.steps[0] and res.ks[1] == ra.ks[0] and res.t[1] == ra.t[0]
+    # Δt of the aborting simulation: 0.01 halved until below 1e-3 (four failures), then inactive
+    dts0 = [c[1][0] for c in eng.calls if c[0] == "dt" and c[2][0]]
+    assert dts0 == [0.01, 0.01, 0.01, 0.005, 0.0025, 0.00125]
+    rb = [c[1][0] for c in eng.calls if c[0] == "rollback"]
+    assert sum(rb) == 4
+    commits0 = [c[1][0] for c in eng.calls if c[0] == "commit"]
+    assert sum(commits0) == 2
+
+
+def test_single_simulation_abort_raises(eb):
+    """run_simulation (one configuration) raises like the reference's error("Simulation aborted.")."""
+    from endobeams_gb300 import api
+    p = eb.SimulationParams(alpha=-0.05, beta=0.28, gamma=0.55, initial_timestep=0.01, min_timestep=1e-3,
+                            max_timestep=0.02, simulation_end_time=0.1, max_iterations=20)
+    res = api.run_simulations([None], p, engine=_ScriptedEngine([[21] * 20]))
+    assert res.aborted == [True] and res.steps == [0]

@@ -25,11 +25,12 @@ def _worker(rank, world, port, q):
     sys.path.insert(0, ROOT)
     import bench
     r, w = bench.dist_init()
+    dev = bench.DEVICE
     bench.barrier(w)
     mx = bench.allreduce_max(float(10 * (r + 1)), w)
     wl = bench.Workload("stents64", rank=r, world=w)
     shard = [tuple(sorted(v.items())) for v in wl.variants]
-    q.put((r, w, mx, shard))
+    q.put((r, w, mx, shard, dev))
     import torch.distributed as dist
     dist.destroy_process_group()
 
@@ -47,6 +48,7 @@ def test_two_gloo_ranks_barrier_and_max():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert [o[:3] for o in out] == [(0, 2, 20.0), (1, 2, 20.0)]
+    assert [o[4] for o in out] == [None, None]  # no GPU visible here: nothing is bound
     # shards: 64 stents each, disjoint, together the first 128 of the population, balanced
     sys.path.insert(0, ROOT)
     import __graft_entry__
@@ -57,3 +59,14 @@ def test_two_gloo_ranks_barrier_and_max():
     assert len(a) == len(b) == 64 and not set(a) & set(b) and sorted(a + b) == sorted(pop)
     elems = lambda sh: sum(dict(v)["wires"] * dict(v)["elems_per_wire"] for v in sh)
     assert abs(elems(a) - elems(b)) <= 0.02 * max(elems(a), elems(b))
+
+
+def test_device_binding_per_local_rank():
+    """Each rank binds its local rank's GPU among those it sees; with one device per rank
+    (CUDA_VISIBLE_DEVICES set per rank by the launcher) every rank binds ordinal 0."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert [bench.device_for_rank(r, 8) for r in range(8)] == list(range(8))
+    assert [bench.device_for_rank(r, 1) for r in range(4)] == [0, 0, 0, 0]
+    assert [bench.device_for_rank(r, 2) for r in range(4)] == [0, 1, 0, 1]
+    assert bench.device_for_rank(3, 0) is None

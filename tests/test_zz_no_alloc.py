@@ -1,6 +1,8 @@
 """eb_contact_eval_noalloc: the contact evaluation for callers that cannot
-allocate device memory during a call (code inside CUDA stream capture, hosts
-whose device memory belongs to their own pool allocator, real-time loops).
+allocate device memory during a call (hosts whose device memory belongs to
+their own pool allocator, such as a Julia or PyTorch runtime that has
+reserved most of the GPU, and real-time loops that forbid allocation after
+start-up).
 
 It reads and writes the caller's device buffers and keeps the prefiltered SDF
 coefficients in a fixed device array instead of allocating.  Checked against
@@ -72,6 +74,25 @@ def test_no_alloc_matches_allocating_entry_point(eb):
             assert err.max() <= tol, f"{name}: {err.max():.3e}"
 
 
+def test_no_alloc_analytic_sphere_and_plane(eb):
+    """The analytic surfaces need no SDF array: sphere and plane (the plane reads surf[1] as its
+    axis) give the allocating entry point's records, bit for bit (same kernel, same inputs)."""
+    from states import plane_states
+    props = np.array([1e4, 0.3, 1e-3, 0.5])
+    center, Rs, rb = np.array([0.1, -0.2, 0.3]), 1.0, 0.01
+    sphere = np.zeros(14)
+    sphere[0], sphere[1:4], sphere[4] = 0, center, Rs
+    plane = np.zeros(14)
+    plane[0], plane[1], plane[2] = 2, 1, 0.013
+    for surf, inp in [(sphere, contact_states(256, center, Rs, rb, seed=31)),
+                      (plane, plane_states(256, 1, 0.013, rb, seed=32))]:
+        ref, ref_flags = eb.contact_eval(inp, props, surf)
+        out, flags = _noalloc(eb, inp, props, surf, np.zeros(1))
+        assert np.array_equal(flags, ref_flags)
+        assert ref_flags.sum() > 100
+        assert np.array_equal(out, ref)
+
+
 def test_no_alloc_rejects_grid_above_limit(eb):
     import torch
 
@@ -88,3 +109,27 @@ def test_no_alloc_rejects_grid_above_limit(eb):
                                    C.c_void_p(d.data_ptr()), C.c_void_p(d.data_ptr()), None)
     assert rc == -1
     assert b"EB_NOALLOC_SDF_MAX_COEFS" in L.eb_last_error()
+
+
+@pytest.mark.parametrize("dims", [(2.0 ** 21 + 3, 2.0 ** 21 + 3, 2.0 ** 21 + 3), (float("nan"), 4, 4),
+                                  (float("inf"), 4, 4), (4.5, 4, 4), (0, 4, 4), (-3, 4, 4), (1e30, 1, 1)])
+def test_no_alloc_rejects_bad_dimensions_before_launching(eb, dims):
+    """Dimensions whose padded product would overflow, non-finite or fractional dimensions are
+    rejected on the host: the output buffer keeps its sentinel, so nothing was launched."""
+    import torch
+
+    from endobeams_gb300 import _lib
+    L = _lib.load()
+    surf = np.zeros(14)
+    surf[0] = 1
+    surf[5:8] = dims
+    surf[11:14] = 0.1
+    d = torch.full((301,), 7.0, dtype=torch.float64, device="cuda")
+    fl = torch.full((1,), 9, dtype=torch.int32, device="cuda")
+    rc = L.eb_contact_eval_noalloc(1, C.c_void_p(d.data_ptr()), _lib.ptr(np.ascontiguousarray(eb.GAUSS)),
+                                   _lib.ptr(np.zeros(4)), _lib.ptr(surf), C.c_void_p(d.data_ptr()),
+                                   C.c_void_p(d.data_ptr()), C.c_void_p(fl.data_ptr()), None)
+    torch.cuda.synchronize()
+    assert rc == -1
+    assert b"eb_contact_eval_noalloc" in L.eb_last_error()
+    assert torch.all(d == 7.0) and int(fl[0]) == 9
