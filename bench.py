@@ -86,6 +86,12 @@ def parse():
     ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
     ap.add_argument("--warm-start", default=None, choices=[None, "off", "learned"])
     ap.add_argument("--count", type=int, default=None, help="population size override (stents)")
+    ap.add_argument("--band-lu", default="fp32", choices=["fp32", "tensor"],
+                    help="band LU engine of the stents' preconditioner")
+    ap.add_argument("--refactor", default="threshold", choices=["threshold", "cost", "always"],
+                    help="stents: when a band LU is refactorised")
+    ap.add_argument("--refactor-cost", type=float, default=0.2,
+                    help="--refactor cost: GMRES iterations one LU is worth per DOF of half bandwidth")
     ap.add_argument("--mem-frac", type=float, default=0.75, help="device memory fraction per resident group")
     ap.add_argument("--cpu-sample", type=int, default=2, help="simulations in the CPU-baseline sample of the GPU arm")
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps per simulation in that CPU-baseline sample")
@@ -116,13 +122,20 @@ def stent_tol_res(conf):
     return STENT_TOL_RES if le >= STENT_ELEM_1E8 else STENT_TOL_RES_SHORT
 
 
+SOLVER = dict(band_lu="fp32", refactor="threshold", refactor_cost=0.2)  # set from the command line
+
+
 def stent_params(p, precision="mixed", warm="off"):
     p.tolerance_residual = STENT_TOL_RES
     p.tolerance_displacement = STENT_TOL_DISP
     p.krylov_restart = 32
-    # the stents' band LU costs ~0.1-1 s per factorisation on one SM: reuse it while GMRES needs <= 200
-    # iterations (64 stents: 20.1 HHT steps/s never refactorising, 17.9 at 48, 14.5 at 16)
-    p.refactor_its = 200
+    # the stents' band LU costs ~0.1-1 s per factorisation on one SM with the FP32 engine: reuse it
+    # while GMRES needs <= 200 iterations (64 stents: 20.1 HHT steps/s never refactorising, 17.9 at
+    # 48, 14.5 at 16), or by the cost rule (iterations lost to ageing against the LU's cost)
+    p.refactor_its = 0 if SOLVER["refactor"] == "always" else 200
+    p.refactor_policy = "cost" if SOLVER["refactor"] == "cost" else "threshold"
+    p.refactor_cost = SOLVER["refactor_cost"]
+    p.band_lu = SOLVER["band_lu"]
     p.linear_tol = NEWTON_FORCING
     p.precision = precision
     p.warm_start = warm
@@ -237,7 +250,7 @@ class Workload:
                    STENT_TOL_DISP)
         return {"workload": w, "sims": self.count, "nodes": int(nodes), "elements": int(elements),
                 "resident_groups": groups, "tolerance_residual": tol[0], "tolerance_displacement": tol[1],
-                "linear_tol": NEWTON_FORCING,
+                "linear_tol": NEWTON_FORCING, "band_lu": SOLVER["band_lu"], "refactor": SOLVER["refactor"],
                 "precision": self.precision, "warm_start": self.warm}
 
 
@@ -726,6 +739,7 @@ def allreduce_max(x, world):
 
 def main():
     args = parse()
+    SOLVER.update(band_lu=args.band_lu, refactor=args.refactor, refactor_cost=args.refactor_cost)
     rank, world = dist_init(bind=args.impl != "reference")
     if args.impl == "reference":
         if rank != 0:

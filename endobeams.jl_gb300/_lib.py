@@ -38,6 +38,7 @@ class EbParams(C.Structure):
         ("preconditioner", C.c_int32), ("refactor_its", C.c_int32), ("stage_band", C.c_int32),
         ("warm_start", C.c_int32), ("use_graph", C.c_int32),
         ("forcing", C.c_int32), ("forcing_max", C.c_double),
+        ("refactor_policy", C.c_int32), ("band_lu", C.c_int32), ("refactor_cost", C.c_double),
     ]
 
 
@@ -105,6 +106,7 @@ SIGNATURES = {
     "eb_set_loads_all": (C.c_int, [C.c_void_p, P_d]),
     "eb_get_displacements": (C.c_int, [C.c_void_p, P_d]),
     "eb_fp64_peak": (C.c_int, [P_d]),
+    "eb_umma_selftest": (C.c_int, [P_f, P_f, C.c_int32, C.c_int32, P_f]),
     "eb_beam_output": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P_d]),
     "eb_autotune": (C.c_int, [C.c_void_p, P_i32]),
     "eb_sdf_from_mesh": (C.c_int, [C.c_int64, P_d, C.c_int64, P_i64, P_i64, P_d, P_d, P_d]),

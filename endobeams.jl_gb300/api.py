@@ -349,6 +349,9 @@ class SimulationParams:
     timing: bool = False             # per-phase CUDA-event timing inside each step
     preconditioner: str = "band"     # "band" (FP32 band LU, RCM order) | "block_jacobi"
     refactor_its: int = 16           # reuse the band LU until a solve needs more GMRES iterations (0: always refactor)
+    refactor_policy: str = "threshold"  # "threshold" (refactor_its only) | "cost" (excess iterations vs LU cost)
+    refactor_cost: float = 0.2       # "cost": GMRES iterations one band LU is worth per DOF of half bandwidth
+    band_lu: str = "fp32"            # "fp32" (CUDA cores) | "tensor" (trailing updates on the tensor cores)
     stage_band: int = 1              # 1: stream band blocks into shared memory with bulk async copies; 0: off;
                                      # 2: test of the bounded wait (the first block's wait runs out)
     warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start)
@@ -376,6 +379,9 @@ class SimulationParams:
         p.timing = 1 if self.timing else 0
         p.preconditioner = 1 if self.preconditioner == "block_jacobi" else 0
         p.refactor_its = int(self.refactor_its)
+        p.refactor_policy = {"threshold": 0, "cost": 1}[self.refactor_policy]
+        p.refactor_cost = float(self.refactor_cost)
+        p.band_lu = {"fp32": 0, "tensor": 1}[self.band_lu]
         p.stage_band = int(self.stage_band)
         if self.warm_start not in ("off", "learned"):
             raise ValueError("warm_start must be 'off' or 'learned'")

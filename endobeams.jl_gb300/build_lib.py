@@ -15,8 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libendobeams_gb300.so")
-SOURCES = ["eb_kernels.cu", "eb_gmres.cu", "eb_band.cu", "eb_abi.cu", "eb_testing.cu", "eb_mlp.cu", "eb_warm.cu",
-           "eb_output.cu", "eb_mesh_sdf.cu"]
+SOURCES = ["eb_kernels.cu", "eb_gmres.cu", "eb_band.cu", "eb_band_tc.cu", "eb_abi.cu", "eb_testing.cu", "eb_mlp.cu",
+           "eb_warm.cu", "eb_output.cu", "eb_mesh_sdf.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

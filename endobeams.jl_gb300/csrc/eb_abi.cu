@@ -391,6 +391,7 @@ struct eb_handle {
   // band-LU preconditioner
   bool any_band = false, any_jacobi = false;
   int max_b = 0;
+  bool tc_lu = false;  // band LU trailing updates on the tensor cores
   size_t band_floats = 0;
   BandDev band{};
   int* d_blk_row = nullptr;
@@ -399,6 +400,9 @@ struct eb_handle {
   int* d_refactor = nullptr;
   std::vector<int> need_refactor, refactor_mask;
   std::vector<double> dt_at_factor, cur_dt;
+  std::vector<int> its0;        // GMRES iterations of the first corrector solve after the factorisation (-1: none yet)
+  std::vector<double> excess;   // iterations spent beyond its0 since the factorisation
+  std::vector<double> lu_cost;  // the band LU's cost in GMRES iterations (refactor_cost * b)
   std::vector<int> cur_active;
   int64_t factorizations = 0;
 };
@@ -433,18 +437,32 @@ int upload_mask(eb_handle* h, int* dst, const int32_t* mask) {
 bool plan_refactor(eb_handle* h, const int* mask) {
   bool any = false;
   if (!h->any_band) return false;
+  double cmax = 0.0;  // largest LU cost among the simulations that refactorise
   for (int s = 0; s < h->n_sims; ++s) {
     int r = 0;
     if (mask[s] && h->band_b[s] > 0)
       r = h->need_refactor[s] || h->dt_at_factor[s] != h->cur_dt[s] || h->P.refactor_its <= 0;
     h->refactor_mask[s] = r;
     if (r) {
-      h->need_refactor[s] = 0;
-      h->dt_at_factor[s] = h->cur_dt[s];
-      ++h->factorizations;
+      cmax = std::max(cmax, h->lu_cost[s]);
       any = true;
     }
   }
+  // One launch factorises every marked simulation; its duration is set by the costliest one,
+  // so simulations half-way to their own limit and no costlier join at no extra wall time.
+  if (any && h->P.refactor_policy == EB_REFACTOR_COST)
+    for (int s = 0; s < h->n_sims; ++s)
+      if (!h->refactor_mask[s] && mask[s] && h->band_b[s] > 0 && h->its0[s] >= 0 && h->lu_cost[s] <= cmax &&
+          h->excess[s] >= 0.5 * h->lu_cost[s])
+        h->refactor_mask[s] = 1;
+  for (int s = 0; s < h->n_sims; ++s)
+    if (h->refactor_mask[s]) {
+      h->need_refactor[s] = 0;
+      h->dt_at_factor[s] = h->cur_dt[s];
+      h->its0[s] = -1;
+      h->excess[s] = 0.0;
+      ++h->factorizations;
+    }
   return any;
 }
 
@@ -469,7 +487,8 @@ int launch_solve(eb_handle* h, bool refactor, const int* refactor_src, PhaseTime
   if (refactor) {
     CK(cudaMemcpyAsync(h->d_refactor, refactor_src, sizeof(int) * h->n_sims, cudaMemcpyHostToDevice, h->stream));
     launch_band_fill(h->d, h->band, h->d_blk_row, h->stream);
-    CK(launch_band_lu(h->d, h->band, h->max_b, h->stream));
+    if (h->tc_lu) CK(launch_band_lu_tc(h->d, h->band, h->max_b, h->band.lu_fail, h->stream));
+    else CK(launch_band_lu(h->d, h->band, h->max_b, h->stream));
     T.launches[EB_PHASE_PRECOND] += 3;
   }
   CK(cudaGetLastError());
@@ -500,9 +519,12 @@ int solve(eb_handle* h, const int* mask, bool corrector) {
 int record_iteration(eb_handle* h, bool refactor, PhaseTimer& T);
 
 // After a bounded bulk-copy wait ran out: band blocks are read from global memory from now on.
+// ... and, after a bounded wait of the tensor-core factorisation ran out, the FP32 factorisation
+// is used from now on.
 void disable_staging(eb_handle* h) {
   h->sa.stage_floats = 0;
   for (SolverArgs& c : h->gclass) c.stage_floats = 0;
+  h->tc_lu = false;
 }
 
 // Launches the captured corrector iteration (capturing it on first use).
@@ -618,6 +640,9 @@ int eb_default_params(eb_params* p) {
   p->use_graph = 1;
   p->forcing = EB_FORCING_FIXED;
   p->forcing_max = 1e-2;
+  p->refactor_policy = EB_REFACTOR_THRESHOLD;
+  p->refactor_cost = 0.2;
+  p->band_lu = EB_LU_FP32;
   return EB_OK;
 }
 
@@ -1113,6 +1138,9 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     CK(A.alloc(&p_li, inv));
     CK(A.alloc(&p_ui, inv));
     CK(A.alloc(&h->d_refactor, n_sims));
+    int* p_lu_fail;
+    CK(A.alloc(&p_lu_fail, n_sims));
+    CK(cudaMemset(p_lu_fail, 0, sizeof(int) * n_sims));
     // CTA order of the per-simulation kernels: decreasing n (b + 1) (band solve and LU work)
     std::vector<int> order(n_sims);
     for (int s = 0; s < n_sims; ++s) order[s] = s;
@@ -1120,11 +1148,17 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
     int* p_order;
     CK(A.upload(&p_order, order));
-    h->band = BandDev{p_band, p_boff, p_bw, p_pos, p_nat, p_work, p_li, p_ui, h->d_refactor, p_order};
+    h->band = BandDev{p_band, p_boff, p_bw, p_pos, p_nat, p_work, p_li, p_ui, h->d_refactor, p_order, p_lu_fail};
+    // the tensor-core factorisation where its shared memory fits the widest band
+    h->tc_lu = h->any_band && p->band_lu == EB_LU_TENSOR && band_lu_tc_smem(h->max_b) <= kGmresSmemLimit;
     sa.band = h->band;
     sa.cta_sim = p_order;
     h->need_refactor.assign(n_sims, 1);
     h->refactor_mask.assign(n_sims, 0);
+    h->its0.assign(n_sims, -1);
+    h->excess.assign(n_sims, 0.0);
+    h->lu_cost.assign(n_sims, 0.0);
+    for (int s = 0; s < n_sims; ++s) h->lu_cost[s] = p->refactor_cost * h->band_b[s];
     h->dt_at_factor.assign(n_sims, 0.0);
     h->cur_dt.assign(n_sims, 0.0);
     h->cur_active.assign(n_sims, 0);
@@ -1656,6 +1690,13 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
         continue;
       }
       if (h->P.refactor_its > 0 && q[4] > h->P.refactor_its) h->need_refactor[s] = 1;
+      if (h->P.refactor_policy == EB_REFACTOR_COST && h->band_b.size() && h->band_b[s] > 0) {
+        // rent or buy: iterations beyond the fresh factorisation's, summed, against the LU's cost
+        const int its_s = (int)q[4];
+        if (h->its0[s] < 0) h->its0[s] = its_s;
+        else h->excess[s] += std::max(0, its_s - h->its0[s]);
+        if (h->excess[s] >= h->lu_cost[s]) h->need_refactor[s] = 1;
+      }
       // compute_norms_corrector (utils_solver.jl:126-151)
       double dnorm = std::sqrt(q[0]);
       double rn = std::sqrt(q[1]);

@@ -28,6 +28,7 @@ __global__ void k_band_fill(Dev d, BandDev B, const int* __restrict__ blk_row) {
 __global__ void k_band_zero(Dev d, BandDev B) {
   const int s = blockIdx.x;
   if (!d.active[s] || !B.refactor[s] || B.bw[s] == 0) return;
+  if (threadIdx.x == 0 && B.lu_fail) B.lu_fail[s] = 0;
   float* A = B.A + B.off[s];
   const int64_t len = band_floats(6 * (d.sim_node_off[s + 1] - d.sim_node_off[s]), B.bw[s]);
   for (int64_t i = threadIdx.x; i < len; i += blockDim.x) A[i] = 0.f;

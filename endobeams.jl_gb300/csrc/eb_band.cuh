@@ -33,6 +33,7 @@ struct BandDev {
   const int* refactor;      // per sim: 1 = refill and refactorise before this solve
   const int* order;         // CTA b of the per-simulation kernels works on simulation order[b]
                             // (largest first, so the last wave holds the smallest simulations)
+  int* lu_fail;             // per sim: 1 = the tensor-core factorisation stopped (a bounded wait ran out)
 };
 
 constexpr int kPanel = 32;     // panel width of the blocked factorisation and solves
@@ -368,5 +369,9 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
 
 void launch_band_fill(const Dev& d, const BandDev& B, const int* blk_row, cudaStream_t s);
 cudaError_t launch_band_lu(const Dev& d, const BandDev& B, int max_b, cudaStream_t s);
+// The same factorisation with the trailing updates on the tensor cores (eb_band_tc.cu); its
+// shared memory for the widest band of the launch is band_lu_tc_smem(max_b).
+cudaError_t launch_band_lu_tc(const Dev& d, const BandDev& B, int max_b, int* lu_fail, cudaStream_t s);
+size_t band_lu_tc_smem(int max_b);
 
 }  // namespace eb

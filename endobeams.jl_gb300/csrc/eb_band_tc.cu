@@ -1,0 +1,385 @@
+// Band LU with the trailing update on the fifth-generation tensor cores.
+//
+// Same factorisation as k_band_lu (eb_band.cu): blocked right-looking LU
+// without pivoting of one simulation's FP32 band, one CTA per simulation,
+// panels of 32 columns.  Per panel:
+//   1. the panel (rows k0 .. k0+32+q) is factorised in shared memory (FP32);
+//   2. U12 = L11⁻¹ A12, one thread per column, written back to the band and,
+//      split into BF16 pairs (hi + lo), into the B operand in shared memory;
+//   3. the L11 / U11 inverses for the triangular solves;
+//   4. A22 -= L21 U12 (q x q, K = 32) on the tensor cores: L21 is split into
+//      BF16 pairs 128 rows at a time (A operand), each 128 x 128 output tile
+//      is the sum of three BF16 products hi·hi + hi·lo + lo·hi accumulated in
+//      FP32 in tensor memory (relative error of a product ~1e-5, against FP32's
+//      6e-8 — the factors are only the GMRES preconditioner), and the
+//      epilogue warps read the tile from tensor memory and update the band in
+//      global memory (each warp's 32 lanes are 32 consecutive rows, so every
+//      column's update is one coalesced 128-byte access).  Tile t+1's MMAs run
+//      on the tensor core while the warps update tile t (two accumulators).
+// The MMA completion waits are bounded: when one runs out the simulation's
+// flag in `lu_fail` is set, the kernel waits (bounded) for its MMAs still in
+// flight, releases its tensor memory and stops; the solver then reports the
+// step not converged and the handle goes back to the FP32 kernel.
+#include "../../include/endobeams_gb300.h"
+#include "eb_band.cuh"
+#include "eb_umma.cuh"
+
+namespace eb {
+
+namespace {
+
+constexpr int kTcThreads = 256;  // 8 warps: warp w updates lanes 32 (w % 4) .., columns 64 (w / 4) ..
+constexpr int kTile = 128;       // M = N = 128 per MMA
+constexpr uint32_t kTmemCols = 2 * kTile;
+constexpr int kOpBytes = kTile * 64;  // one 128-row, 32-wide-K BF16 operand tile (hi or lo)
+
+// Shared memory of one CTA for half bandwidth b (bytes): mbarriers and the tensor-memory slot,
+// the FP32 panel ((32 + b) x 32, odd column stride), the B operand (hi and lo, q <= b columns
+// rounded up to 128) and one A operand chunk (hi and lo).
+__host__ __device__ inline size_t tc_ldp(int b) { return (size_t)kPanel + b; }
+__host__ __device__ inline size_t tc_npad(int b) { return ((size_t)b + kTile - 1) / kTile * kTile; }
+__host__ __device__ inline size_t tc_smem_bytes(int b) {
+  return 1024 + sizeof(float) * tc_ldp(b) * kPanel + 2 * 64 * tc_npad(b) + 2 * (size_t)kOpBytes;
+}
+
+__device__ __forceinline__ void store_pair(char* hi, char* lo, uint32_t off, const float (&x)[8]) {
+  __nv_bfloat16 h[8], l[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) umma::split_bf16(x[j], h[j], l[j]);
+  *reinterpret_cast<uint4*>(hi + off) = *reinterpret_cast<const uint4*>(h);
+  *reinterpret_cast<uint4*>(lo + off) = *reinterpret_cast<const uint4*>(l);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int* lu_fail) {
+  const int s = B.order[blockIdx.x];
+  if (!d.active[s] || !B.refactor[s]) return;
+  const int b = B.bw[s];
+  if (b == 0) return;
+  const int64_t n0 = d.sim_node_off[s];
+  const int n = (int)(6 * (d.sim_node_off[s + 1] - n0));
+  const BandView V = band_view(B, s, n);
+  float* Li = B.Linv + inv_base(n0, s);
+  float* Ui = B.Uinv + inv_base(n0, s);
+  extern __shared__ __align__(1024) char smc[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smc);          // two MMA-completion barriers
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smc + 64);   // tensor-memory base address
+  int* sfail = reinterpret_cast<int*>(smc + 128);
+  const int ldp = (int)tc_ldp(b);
+  float* P = reinterpret_cast<float*>(smc + 1024);                        // panel, ldp x 32 column-major
+  char* Bhi = reinterpret_cast<char*>(P + (size_t)ldp * kPanel);          // B operand: q columns (N), K = 32
+  const size_t npad = tc_npad(b);
+  char* Blo = Bhi + 64 * npad;
+  char* Ahi = Blo + 64 * npad;                                            // A operand chunk: 128 rows (M)
+  char* Alo = Ahi + kOpBytes;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nw = kTcThreads / 32;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    *sfail = 0;
+    fence_async_smem();
+  }
+  if (warp == 0) umma::tmem_alloc(tslot, kTmemCols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = umma::idesc_bf16_f32(kTile, kTile);
+  uint32_t phase[2] = {0u, 0u};  // next completion parity of each accumulator's barrier
+  int pending[2] = {0, 0};       // thread 0: commits not yet waited for
+  bool failed = false;
+
+  for (int k0 = 0; k0 < n && !failed; k0 += kPanel) {
+    const int kb = min(kPanel, n - k0);
+    const int hp = min(n - k0, kb + b);
+    const int q = min(n - k0 - kb, b);
+    // ---- load the panel (column c = lane, rows strided by warps)
+    if (lane < kb)
+      for (int r = warp; r < hp; r += nw) {
+        const int i = k0 + r, j = k0 + lane;
+        P[r + ldp * lane] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
+      }
+    __syncthreads();
+    // ---- 1. panel LU (column c = lane)
+    for (int t = 0; t < kb; ++t) {
+      const float ip = 1.f / P[t + ldp * t];
+      for (int r = t + 1 + threadIdx.x; r < hp; r += kTcThreads) P[r + ldp * t] *= ip;
+      __syncthreads();
+      if (lane > t && lane < kb) {
+        const float ut = P[t + ldp * lane];
+        for (int r = t + 1 + warp; r < hp; r += nw) P[r + ldp * lane] -= P[r + ldp * t] * ut;
+      }
+      __syncthreads();
+    }
+    // ---- 2. U12 = L11⁻¹ A12 (thread per column; q > 0 implies kb = 32), into the band and B
+    for (int c = threadIdx.x; c < q; c += kTcThreads) {
+      // entries of A12 with j - i > b lie outside the band: zero, and not written back
+      const int rlo = max(0, kPanel + c - b);
+      float col[kPanel];
+#pragma unroll
+      for (int r = 0; r < kPanel; ++r) col[r] = r >= rlo ? V.at(k0 + r, k0 + kPanel + c) : 0.f;
+#pragma unroll
+      for (int r = 1; r < kPanel; ++r) {
+        float acc = col[r];
+#pragma unroll
+        for (int t = 0; t < r; ++t) acc -= P[r + ldp * t] * col[t];
+        col[r] = acc;
+      }
+#pragma unroll
+      for (int r = 0; r < kPanel; ++r)
+        if (r >= rlo) V.at(k0 + r, k0 + kPanel + c) = col[r];
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        float x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = col[8 * g + j];
+        store_pair(Bhi, Blo, umma::kmajor_offset(c, 8 * g), x);
+      }
+    }
+    // B columns past q (up to the 128-column tile) are zero
+    for (int c = q + threadIdx.x; c < (int)((q + kTile - 1) / kTile * kTile); c += kTcThreads) {
+      const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int g = 0; g < 4; ++g) store_pair(Bhi, Blo, umma::kmajor_offset(c, 8 * g), z);
+    }
+    // ---- 3. inverses of L11 (unit lower) and U11 (upper), as k_band_lu
+    if (warp == 0) {
+      float z[kPanel];
+#pragma unroll
+      for (int r = 0; r < kPanel; ++r) {
+        float acc = (r == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int t = 0; t < r; ++t) acc -= (r < kb && t < kb ? P[r + ldp * t] : 0.f) * z[t];
+        z[r] = acc;
+      }
+      float* L = Li + (int64_t)k0 * kPanel;
+#pragma unroll
+      for (int r = 0; r < kPanel; ++r) L[lane * kPanel + r] = z[r];
+    } else if (warp == 1) {
+      float z[kPanel];
+#pragma unroll
+      for (int r = kPanel - 1; r >= 0; --r) {
+        float acc = (r == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int t = r + 1; t < kPanel; ++t) acc -= (r < kb && t < kb ? P[r + ldp * t] : 0.f) * z[t];
+        z[r] = r < kb ? acc / P[r + ldp * r] : acc;
+      }
+      float* Uv = Ui + (int64_t)k0 * kPanel;
+#pragma unroll
+      for (int r = 0; r < kPanel; ++r) Uv[lane * kPanel + r] = z[r];
+    }
+    // ---- write back the panel (L11, U11, L21)
+    if (lane < kb)
+      for (int r = warp; r < hp; r += nw) {
+        const int i = k0 + r, j = k0 + lane;
+        if (i - j <= b && j - i <= b) V.at(i, j) = P[r + ldp * lane];
+      }
+    __syncthreads();
+    if (q <= 0) continue;
+    // ---- 4. A22 -= L21 U12 on the tensor cores, 128 x 128 tiles, M chunk by M chunk
+    const int mt = (q + kTile - 1) / kTile, nt = mt;
+    for (int mc = 0; mc < mt && !failed; ++mc) {
+      // A operand: rows 128 mc .. of L21 (panel rows 32 + m), split into BF16 pairs; rows past q are zero
+      for (int u = threadIdx.x; u < kTile * 4; u += kTcThreads) {
+        const int ml = u % kTile, g = u / kTile, m = kTile * mc + ml;
+        float x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = m < q ? P[(kPanel + m) + ldp * (8 * g + j)] : 0.f;
+        store_pair(Ahi, Alo, umma::kmajor_offset(ml, 8 * g), x);
+      }
+      umma::fence_proxy_async();  // operand writes visible to the tensor core
+      umma::fence_before_sync();
+      __syncthreads();
+      umma::fence_after_sync();
+      // tile (mc, nc) accumulates in tensor-memory columns 128 (nc % 2) ..
+      auto issue = [&](int nc) {
+        const uint32_t dt = tmem + (uint32_t)(kTile * (nc & 1));
+        const uint32_t a_hi = umma::smem_addr(Ahi), a_lo = umma::smem_addr(Alo);
+        const uint32_t b_hi = umma::smem_addr(Bhi + (size_t)nc * kOpBytes);
+        const uint32_t b_lo = umma::smem_addr(Blo + (size_t)nc * kOpBytes);
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {  // K = 32 as two MMAs of K = 16
+          const uint32_t o = 256u * ks;
+          umma::mma_bf16(dt, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_hi + o, 128, 512), idesc, ks);
+          umma::mma_bf16(dt, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_lo + o, 128, 512), idesc, 1);
+          umma::mma_bf16(dt, umma::smem_desc(a_lo + o, 128, 512), umma::smem_desc(b_hi + o, 128, 512), idesc, 1);
+        }
+        umma::commit(&bar[nc & 1]);
+        pending[nc & 1] += 1;
+      };
+      if (threadIdx.x == 0) issue(0);
+      for (int nc = 0; nc < nt; ++nc) {
+        const int buf = nc & 1;
+        if (!mbar_wait(&bar[buf], phase[buf])) *sfail = 1;
+        if (threadIdx.x == 0 && !*sfail) pending[buf] -= 1;
+        phase[buf] ^= 1u;
+        umma::fence_after_sync();
+        __syncthreads();
+        if (*sfail) {
+          failed = true;
+          break;
+        }
+        // the next tile's MMAs run while this one is written back (its accumulator was
+        // released by the barrier that ended tile nc - 1)
+        if (threadIdx.x == 0 && nc + 1 < nt) issue(nc + 1);
+        const int quarter = warp & 3, half = warp >> 2;
+        const int m = kTile * mc + 32 * quarter + lane;
+        const int i = k0 + kPanel + m;
+#pragma unroll
+        for (int cb = 0; cb < 2; ++cb) {
+          const int c0 = 64 * half + 32 * cb;
+          float acc[32];
+          umma::ld_32cols(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(kTile * buf + c0), acc);
+          if (m < q) {
+            const int jb = k0 + kPanel + kTile * nc + c0;
+            const int cmax = min(32, q - (kTile * nc + c0));
+            float old[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) old[c] = c < cmax ? V.at(i, jb + c) : 0.f;
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+              if (c < cmax) V.at(i, jb + c) = old[c] - acc[c];
+          }
+        }
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+      }
+    }
+    __syncthreads();
+  }
+  if (failed) {
+    // a completion wait ran out: wait (bounded) for the MMAs still in flight before the
+    // tensor memory is released
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < 2; ++k)
+        while (pending[k] > 0) {
+          mbar_wait(&bar[k], phase[k]);
+          phase[k] ^= 1u;
+          pending[k] -= 1;
+        }
+      lu_fail[s] = 1;
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (warp == 0) umma::tmem_dealloc(tmem, kTmemCols);
+}
+
+size_t band_lu_tc_smem(int max_b) { return tc_smem_bytes(max_b); }
+
+cudaError_t launch_band_lu_tc(const Dev& d, const BandDev& B, int max_b, int* lu_fail, cudaStream_t s) {
+  if (max_b <= 0) return cudaSuccess;
+  const size_t smem = tc_smem_bytes(max_b);
+  cudaError_t e = cudaFuncSetAttribute(k_band_lu_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_band_lu_tc<<<d.n_sims, kTcThreads, smem, s>>>(d, B, lu_fail);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- single-tile self-test
+// One CTA of 128 threads: D (128 x N) = A (128 x 32) B (N x 32)ᵀ with the operands rounded to
+// BF16 (split = 0) or split into BF16 pairs with the three-product sum of the band LU (split = 1).
+__global__ void k_umma_selftest(const float* __restrict__ A, const float* __restrict__ Bm, int N, int split,
+                                float* __restrict__ D, int* status) {
+  extern __shared__ __align__(1024) char smc[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smc);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smc + 64);
+  char* Ahi = smc + 1024;
+  char* Alo = Ahi + kOpBytes;
+  char* Bhi = Alo + kOpBytes;
+  char* Blo = Bhi + 2 * kOpBytes;  // N <= 256 rows
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int u = threadIdx.x; u < kTile * 4; u += blockDim.x) {
+    const int r = u % kTile, g = u / kTile;
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = A[r * 32 + 8 * g + j];
+    store_pair(Ahi, Alo, umma::kmajor_offset(r, 8 * g), x);
+  }
+  for (int u = threadIdx.x; u < N * 4; u += blockDim.x) {
+    const int r = u % N, g = u / N;
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = Bm[r * 32 + 8 * g + j];
+    store_pair(Bhi, Blo, umma::kmajor_offset(r, 8 * g), x);
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    fence_async_smem();
+  }
+  if (warp == 0) umma::tmem_alloc(tslot, 256);
+  umma::fence_proxy_async();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  if (threadIdx.x == 0) {
+    const uint32_t idesc = umma::idesc_bf16_f32(kTile, N);
+    const uint32_t a_hi = umma::smem_addr(Ahi), a_lo = umma::smem_addr(Alo);
+    const uint32_t b_hi = umma::smem_addr(Bhi), b_lo = umma::smem_addr(Blo);
+    for (int ks = 0; ks < 2; ++ks) {
+      const uint32_t o = 256u * ks;
+      umma::mma_bf16(tmem, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_hi + o, 128, 512), idesc, ks);
+      if (split) {
+        umma::mma_bf16(tmem, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_lo + o, 128, 512), idesc, 1);
+        umma::mma_bf16(tmem, umma::smem_desc(a_lo + o, 128, 512), umma::smem_desc(b_hi + o, 128, 512), idesc, 1);
+      }
+    }
+    umma::commit(&bar[0]);
+  }
+  const bool ok = mbar_wait(&bar[0], 0);
+  umma::fence_after_sync();
+  if (ok) {
+    for (int c0 = 0; c0 < N; c0 += 32) {
+      float acc[32];
+      umma::ld_32cols(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
+      const int r = 32 * warp + lane;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) D[(int64_t)r * N + c0 + c] = acc[c];
+    }
+  } else if (threadIdx.x == 0) {
+    *status = 1;
+    mbar_wait(&bar[0], 0);  // bounded second wait for the MMAs in flight
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (warp == 0) umma::tmem_dealloc(tmem, 256);
+}
+
+}  // namespace eb
+
+extern "C" int eb_umma_selftest(const float* A, const float* B, int32_t N, int32_t split, float* D) {
+  using namespace eb;
+  if (!A || !B || !D || !(N == 64 || N == 128 || N == 256)) return EB_ERR_ARG;
+  float *dA = nullptr, *dB = nullptr, *dD = nullptr;
+  int* dst = nullptr;
+  int st = 0;
+  cudaError_t e = cudaSuccess;
+  const size_t smem = 1024 + 2 * (size_t)kOpBytes + 4 * (size_t)kOpBytes;
+  if ((e = cudaMalloc(&dA, sizeof(float) * 128 * 32)) == cudaSuccess &&
+      (e = cudaMalloc(&dB, sizeof(float) * (size_t)N * 32)) == cudaSuccess &&
+      (e = cudaMalloc(&dD, sizeof(float) * 128 * (size_t)N)) == cudaSuccess &&
+      (e = cudaMalloc(&dst, sizeof(int))) == cudaSuccess &&
+      (e = cudaMemcpy(dA, A, sizeof(float) * 128 * 32, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (e = cudaMemcpy(dB, B, sizeof(float) * (size_t)N * 32, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (e = cudaMemset(dst, 0, sizeof(int))) == cudaSuccess &&
+      (e = cudaFuncSetAttribute(k_umma_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) ==
+          cudaSuccess) {
+    k_umma_selftest<<<1, 128, smem>>>(dA, dB, N, split, dD, dst);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(D, dD, sizeof(float) * 128 * (size_t)N, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dD);
+  cudaFree(dst);
+  if (e != cudaSuccess) return EB_ERR_CUDA;
+  return st ? EB_ERR_CUDA : EB_OK;
+}

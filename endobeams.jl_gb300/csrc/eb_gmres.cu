@@ -155,6 +155,8 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   double rnorm = bnorm;
   int its = 0, refs = 0, status = 0;
   if (!isfinite(bnorm)) status = 2;  // EB_SIM_NAN
+  // the tensor-core factorisation of these factors stopped at a bounded wait: not trusted
+  if (use_band && a.band.lu_fail && a.band.lu_fail[s]) status = 4;
 
   // relative tolerance of this solve (inexact Newton, Eisenstat-Walker choice 2)
   double rtol = a.tol;

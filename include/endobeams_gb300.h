@@ -90,7 +90,24 @@ typedef struct {
                                              EB_FORCING_EW: inexact Newton, Eisenstat-Walker forcing terms */
   double forcing_max;                     /* EB_FORCING_EW: largest relative tolerance of a solve (also the
                                              predictor's); linear_tol is the smallest */
+  int32_t refactor_policy;                /* EB_REFACTOR_THRESHOLD | EB_REFACTOR_COST (refactor_its stays a cap) */
+  int32_t band_lu;                        /* EB_LU_FP32 | EB_LU_TENSOR */
+  double refactor_cost;                   /* EB_REFACTOR_COST: GMRES iterations one band LU is worth, per
+                                             DOF of half bandwidth (the LU does N b^2 work, an iteration N b) */
 } eb_params;
+
+/* Band LU engine */
+#define EB_LU_FP32 0    /* FP32 on the CUDA cores */
+#define EB_LU_TENSOR 1  /* panels in FP32, trailing updates on the tensor cores as sums of three BF16
+                           products (operands split into BF16 pairs, FP32 accumulation); the FP32 engine
+                           where the band is too wide for its shared memory (b > ~800) */
+
+/* When a simulation's band LU is refactorised (besides missing factors and a changed Δt) */
+#define EB_REFACTOR_THRESHOLD 0  /* a solve needed more than refactor_its GMRES iterations */
+#define EB_REFACTOR_COST 1       /* the GMRES iterations spent beyond those of the first solve after the
+                                    factorisation, summed, reach refactor_cost * b (the LU's own cost in
+                                    iterations): a rent-or-buy rule per simulation; when any simulation
+                                    refactorises, those already half-way to their own limit join it */
 
 /* Linear-solve tolerance per Newton iteration */
 #define EB_FORCING_FIXED 0  /* linear_tol for every solve (the reference's direct solve, approximated) */
@@ -294,6 +311,12 @@ int eb_contact_eval(int64_t n, const double *in, const double *gauss6, const dou
 int eb_contact_eval_noalloc(int64_t n, const double *d_in, const double *gauss6, const double *props,
                             const double *surf, const double *d_sdf_values, double *d_out, int32_t *d_flags,
                             void *stream);
+
+/* Tensor-core self-test (no reference counterpart): D (128 x N, row-major) = A (128 x 32) Bᵀ
+ * (B: N x 32), both row-major FP32, on one CTA with the MMA, operand layout and tensor-memory
+ * epilogue of the tensor-core band LU; split = 0 rounds A and B to BF16, split = 1 sums the
+ * three BF16 products of their BF16 pairs.  N is 64, 128 or 256. */
+int eb_umma_selftest(const float *A, const float *B, int32_t N, int32_t split, float *D);
 
 /* Measured FP64 FMA throughput of device 0 in TFLOP/s (independent FMA
  * chains on every SM, CUDA-event timed); the roofline denominator of the
