@@ -55,7 +55,7 @@ class EbSimDesc(C.Structure):
         ("n_contact_elems", C.c_int64), ("contact_elems", P_i64),
         ("sphere_center", C.c_double * 3), ("sphere_radius", C.c_double),
         ("sdf_dims", C.c_int64 * 3), ("sdf_origin", C.c_double * 3), ("sdf_spacing", C.c_double * 3),
-        ("sdf_values", P_d), ("sdf_inside", C.c_int32),
+        ("sdf_values", P_d), ("sdf_inside", C.c_int32), ("sdf_interp", C.c_int32),
         ("plane_axis", C.c_int32), ("plane_position", C.c_double),
     ]
 
@@ -64,7 +64,8 @@ class EbSimStats(C.Structure):
     _fields_ = [
         ("newton_iterations", C.c_int32), ("krylov_iterations", C.c_int32), ("refinements", C.c_int32),
         ("status", C.c_int32), ("last_res_norm", C.c_double), ("last_dD_norm", C.c_double),
-        ("max_linear_rel_residual", C.c_double), ("warm_start_used", C.c_int32), ("reserved", C.c_int32),
+        ("max_linear_rel_residual", C.c_double), ("warm_start_used", C.c_int32),
+        ("predictor_krylov_iterations", C.c_int32),
         ("predictor_rhs_norm", C.c_double), ("start_res_norm", C.c_double),
     ]
 

@@ -183,10 +183,17 @@ class DiscreteSignedDistanceField:
     """DiscreteSignedDistanceField(filename, inside) (def_interactions.jl:67-82).
 
     The grid is kept as given (x fastest); the quadratic B-spline prefilter
-    runs in the library.  ``from_grid`` builds one from an array."""
+    runs in the library.  ``from_grid`` builds one from an array.
+
+    ``interpolation="trilinear"`` (not in the reference) interpolates the
+    samples trilinearly instead (8 taps, no prefilter; the gradient jumps
+    across cell faces and the Hessian keeps only its mixed terms)."""
 
     def __init__(self, filename: Optional[str] = None, inside: bool = True, flag_load_from_file_iterative=False,
-                 *, values=None, origin=None, spacing=None):
+                 *, values=None, origin=None, spacing=None, interpolation: str = "quadratic"):
+        if interpolation not in ("quadratic", "trilinear"):
+            raise ValueError("interpolation must be 'quadratic' or 'trilinear'")
+        self.interpolation = interpolation
         if filename is not None:
             dims, spacing, origin, values = read_vtk_sdf(filename)
             values = np.asarray(values, float).reshape(dims[2], dims[1], dims[0])
@@ -200,8 +207,8 @@ class DiscreteSignedDistanceField:
         self.dom = (self.origin[0], ends[0], self.origin[1], ends[1], self.origin[2], ends[2])
 
     @classmethod
-    def from_grid(cls, values, origin, spacing, inside=True):
-        return cls(None, inside, values=values, origin=origin, spacing=spacing)
+    def from_grid(cls, values, origin, spacing, inside=True, interpolation="quadratic"):
+        return cls(None, inside, values=values, origin=origin, spacing=spacing, interpolation=interpolation)
 
     @classmethod
     def from_mesh(cls, positions, triangles, origin, spacing, dims, inside=True):
@@ -354,7 +361,8 @@ class SimulationParams:
     band_lu: str = "fp32"            # "fp32" (CUDA cores) | "tensor" (trailing updates on the tensor cores)
     stage_band: int = 1              # 1: stream band blocks into shared memory with bulk async copies; 0: off;
                                      # 2: test of the bounded wait (the first block's wait runs out)
-    warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start)
+    warm_start: str = "off"          # "off": HHT predictor; "learned": per-node MLP start (set_warm_start);
+                                     # "learned_x0": HHT predictor with the MLP increment as its GMRES initial guess
     use_graph: bool = True           # replay each Newton iteration from a CUDA graph
     autotune: bool = True            # run_simulations: pick kernel block sizes after the first step
     forcing: str = "fixed"           # "fixed": every solve to linear_tol; "ew": inexact Newton
@@ -383,9 +391,10 @@ class SimulationParams:
         p.refactor_cost = float(self.refactor_cost)
         p.band_lu = {"fp32": 0, "tensor": 1}[self.band_lu]
         p.stage_band = int(self.stage_band)
-        if self.warm_start not in ("off", "learned"):
-            raise ValueError("warm_start must be 'off' or 'learned'")
-        p.warm_start = 1 if self.warm_start == "learned" else 0
+        modes = {"off": 0, "learned": 1, "learned_x0": 2}
+        if self.warm_start not in modes:
+            raise ValueError("warm_start must be 'off', 'learned' or 'learned_x0'")
+        p.warm_start = modes[self.warm_start]
         p.use_graph = int(bool(self.use_graph))
         if self.forcing not in ("fixed", "ew"):
             raise ValueError("forcing must be 'fixed' or 'ew'")
@@ -468,6 +477,7 @@ class GpuSimulations:
                     d.sdf_spacing[i] = m.spacing[i]
                 d.sdf_values = ptr(self._k(f64(m.values)))
                 d.sdf_inside = 1 if m.inside else 0
+                d.sdf_interp = 1 if getattr(m, "interpolation", "quadratic") == "trilinear" else 0
             else:
                 raise NotImplementedError(f"surface {type(m).__name__} has no gap function")
 

@@ -233,6 +233,10 @@ std::vector<double> sdf_coefficients(const double* values, const int64_t dims[3]
 
 }  // namespace
 
+std::vector<double> eb_sdf_samples_padded_host(const double* values, const int64_t dims[3], bool negate) {
+  return sdf_padded(values, dims, negate);
+}
+
 std::vector<double> eb_sdf_coefficients_host(const double* values, const int64_t dims[3], bool negate) {
   return sdf_coefficients(values, dims, negate);
 }
@@ -383,6 +387,8 @@ struct eb_handle {
   float* d_Dinv32 = nullptr;
   double* d_norms = nullptr;
   int *d_its = nullptr, *d_refs = nullptr, *d_status = nullptr;
+  int* d_pred_its = nullptr;  // per sim: GMRES iterations of this step's predictor solve
+  int* d_x0_on = nullptr;     // per sim: the next solve starts from the initial guess in dD
   double* d_relres = nullptr;
   std::vector<eb_sim_stats> stats;
   std::vector<double> h_norms;
@@ -730,6 +736,10 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
         return fail(EB_ERR_ARG, "sim %d: SDF grid missing", s);
       if (S.sdf_spacing[0] <= 0 || S.sdf_spacing[1] <= 0 || S.sdf_spacing[2] <= 0)
         return fail(EB_ERR_ARG, "sim %d: SDF spacing must be positive", s);
+      if (S.sdf_interp != EB_SDF_QUADRATIC && S.sdf_interp != EB_SDF_TRILINEAR)
+        return fail(EB_ERR_ARG, "sim %d: unknown SDF interpolation %d", s, (int)S.sdf_interp);
+      if (S.sdf_interp == EB_SDF_TRILINEAR && (S.sdf_dims[0] < 2 || S.sdf_dims[1] < 2 || S.sdf_dims[2] < 2))
+        return fail(EB_ERR_ARG, "sim %d: a trilinear SDF needs at least 2 points per axis", s);
     }
     h->node_off[s + 1] = h->node_off[s] + S.n_nodes;
     h->elem_off[s + 1] = h->elem_off[s] + S.n_elem;
@@ -824,6 +834,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
         sf.pos = S.plane_position;
       } else if (S.surface == EB_SURFACE_SDF) {
         sf.kind = 1;
+        sf.interp = S.sdf_interp;
         sf.nx = (int)S.sdf_dims[0]; sf.ny = (int)S.sdf_dims[1]; sf.nz = (int)S.sdf_dims[2];
         sf.x0 = S.sdf_origin[0]; sf.y0 = S.sdf_origin[1]; sf.z0 = S.sdf_origin[2];
         sf.ihx = 1.0 / S.sdf_spacing[0]; sf.ihy = 1.0 / S.sdf_spacing[1]; sf.ihz = 1.0 / S.sdf_spacing[2];
@@ -955,7 +966,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
       const eb_sim_desc& S = sims[s];
       for (int t : todo) {
         const eb_sim_desc& T = sims[t];
-        if (T.sdf_values == S.sdf_values && T.sdf_inside == S.sdf_inside &&
+        if (T.sdf_values == S.sdf_values && T.sdf_inside == S.sdf_inside && T.sdf_interp == S.sdf_interp &&
             std::memcmp(T.sdf_dims, S.sdf_dims, sizeof S.sdf_dims) == 0 &&
             std::memcmp(T.sdf_origin, S.sdf_origin, sizeof S.sdf_origin) == 0 &&
             std::memcmp(T.sdf_spacing, S.sdf_spacing, sizeof S.sdf_spacing) == 0) {
@@ -983,7 +994,9 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
         const eb_sim_desc& S = sims[todo[i]];
         double* c;
         CK(A.upload(&c, chunk[i - c0]));
-        launch_sdf_prefilter(c, (int)S.sdf_dims[0], (int)S.sdf_dims[1], (int)S.sdf_dims[2], h->stream);
+        // the trilinear interpolant uses the samples themselves
+        if (S.sdf_interp == EB_SDF_QUADRATIC)
+          launch_sdf_prefilter(c, (int)S.sdf_dims[0], (int)S.sdf_dims[1], (int)S.sdf_dims[2], h->stream);
         CK(cudaGetLastError());
         surf[todo[i]].coef = c;
         std::vector<double>().swap(chunk[i - c0]);
@@ -1099,6 +1112,10 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   sa.forcing_max = p->forcing_max;
   CK(A.alloc(&sa.prev_bnorm, n_sims));
   CK(A.alloc(&sa.prev_eta, n_sims));
+  CK(A.alloc(&h->d_pred_its, n_sims));
+  CK(A.alloc(&h->d_x0_on, n_sims));
+  CK(cudaMemset(h->d_x0_on, 0, sizeof(int) * n_sims));
+  sa.x0_on = h->d_x0_on;
   h->stats.assign(n_sims, eb_sim_stats{});
   h->h_norms.assign(5 * (size_t)n_sims, 0.0);
   h->max_it.assign(n_sims, p->max_iterations);
@@ -1150,7 +1167,7 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
     CK(A.upload(&p_order, order));
     h->band = BandDev{p_band, p_boff, p_bw, p_pos, p_nat, p_work, p_li, p_ui, h->d_refactor, p_order, p_lu_fail};
     // the tensor-core factorisation where its shared memory fits the widest band
-    h->tc_lu = h->any_band && p->band_lu == EB_LU_TENSOR && band_lu_tc_smem(h->max_b) <= kGmresSmemLimit;
+    h->tc_lu = h->any_band && p->band_lu == EB_LU_TENSOR && band_lu_tc_smem(h->max_b) <= kLuTcSmemLimit;
     sa.band = h->band;
     sa.cta_sim = p_order;
     h->need_refactor.assign(n_sims, 1);
@@ -1536,7 +1553,9 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
   const int S = h->n_sims;
   const eb_params& P = h->P;
   const bool learned = P.warm_start == EB_WS_LEARNED;
-  if (learned && !h->ws.model) return fail(EB_ERR_STATE, "eb_step: warm_start is EB_WS_LEARNED but no model is set");
+  const bool learned_x0 = P.warm_start == EB_WS_LEARNED_X0;
+  if ((learned || learned_x0) && !h->ws.model)
+    return fail(EB_ERR_STATE, "eb_step: a learned warm start is selected but no model is set");
   const double a = P.alpha, b = P.beta, g = P.gamma;
   std::vector<double> cK(S), cC(S), cM(S), dts(S);
   std::vector<int> act(S), iter(S, 0), k(S, 1);
@@ -1567,7 +1586,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
 
   // ---- features of the learned start / of the captured samples (committed state)
   WsHost& ws = h->ws;
-  if (learned || ws.cap > 0) {
+  if (learned || learned_x0 || ws.cap > 0) {
     launch_ws_features(d, ws.dev, st);
     T.launches[EB_PHASE_PREDICTOR] += 1;
     ws.features_valid = true;
@@ -1605,10 +1624,20 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
       T.launches[EB_PHASE_PREDICTOR] += 3;
     }
     CK(cudaMemcpyAsync(h->d_active, act.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  } else if (learned_x0) {
+    // the network's increment as the initial guess of the predictor's solve (free DOFs of dD)
+    CK(mlp_forward(MlpDev{ws.P, ws.W}, ws.X, d.n_nodes, ws.Y, st));
+    launch_ws_apply(d, ws.dev, st);
+    T.launches[EB_PHASE_PREDICTOR] += 2;
+    CK(cudaMemcpyAsync(h->d_x0_on, act.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    rc = solve(h, act.data(), false);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(h->d_x0_on, 0, sizeof(int) * S, st));
   } else {
     rc = solve(h, act.data(), false);
     if (rc) return rc;
   }
+  CK(cudaMemcpyAsync(h->d_pred_its, h->d_its, sizeof(int) * S, cudaMemcpyDeviceToDevice, st));
   launch_global_predictor(d, b, g, st);
   launch_local_predictor(d, b, g, st);
   // ---- corrector! (corrector.jl:1-59)
@@ -1718,8 +1747,9 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     }
   }
   // ---- statistics
-  std::vector<int> its(S), refs(S), status(S);
+  std::vector<int> its(S), refs(S), status(S), pred_its(S);
   std::vector<double> rel(S);
+  CK(cudaMemcpyAsync(pred_its.data(), h->d_pred_its, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(its.data(), h->d_its, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(refs.data(), h->d_refs, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(status.data(), h->d_status, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
@@ -1746,6 +1776,7 @@ int eb_step(eb_handle* h, const double* dt, const int32_t* active, int32_t* k_ou
     q.last_dD_norm = dn[s];
     q.max_linear_rel_residual = rel[s];
     q.warm_start_used = learned ? ws.used[s] : 0;
+    q.predictor_krylov_iterations = pred_its[s];
     q.predictor_rhs_norm = learned && ws.tried[s] ? std::sqrt(ws.rn[s]) : 0.0;
     q.start_res_norm = learned && ws.tried[s] ? std::sqrt(ws.rn[S + s]) : 0.0;
     k_out[s] = k[s];

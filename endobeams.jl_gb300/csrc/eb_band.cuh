@@ -373,5 +373,6 @@ cudaError_t launch_band_lu(const Dev& d, const BandDev& B, int max_b, cudaStream
 // shared memory for the widest band of the launch is band_lu_tc_smem(max_b).
 cudaError_t launch_band_lu_tc(const Dev& d, const BandDev& B, int max_b, int* lu_fail, cudaStream_t s);
 size_t band_lu_tc_smem(int max_b);
+constexpr size_t kLuTcSmemLimit = 227 * 1024;  // the opt-in shared memory of one CTA (the kernel has no static part)
 
 }  // namespace eb

@@ -8,14 +8,16 @@
 //      split into BF16 pairs (hi + lo), into the B operand in shared memory;
 //   3. the L11 / U11 inverses for the triangular solves;
 //   4. A22 -= L21 U12 (q x q, K = 32) on the tensor cores: L21 is split into
-//      BF16 pairs 128 rows at a time (A operand), each 128 x 128 output tile
-//      is the sum of three BF16 products hi·hi + hi·lo + lo·hi accumulated in
-//      FP32 in tensor memory (relative error of a product ~1e-5, against FP32's
-//      6e-8 — the factors are only the GMRES preconditioner), and the
-//      epilogue warps read the tile from tensor memory and update the band in
-//      global memory (each warp's 32 lanes are 32 consecutive rows, so every
-//      column's update is one coalesced 128-byte access).  Tile t+1's MMAs run
-//      on the tensor core while the warps update tile t (two accumulators).
+//      three BF16 parts (hi + mid + lo = the FP32 value) 128 rows at a time (A
+//      operand), U12 likewise (B operand), and each 128 x 128 output tile is the
+//      sum of the six BF16 products above FP32's rounding level (mm, lh, hl,
+//      mh, hm, hh, smallest first) accumulated in FP32 in tensor memory — the
+//      rounding of an FP32 product (a two-part split, three products, left the
+//      factors ~1e-5 off and cost 60% more GMRES iterations); the epilogue warps
+//      read the tile from tensor memory and update the band in global memory
+//      (each warp's 32 lanes are 32 consecutive rows, so every column's update
+//      is one coalesced 128-byte access).  Tile t+1's MMAs run on the tensor
+//      core while the warps update tile t (two accumulators).
 // The MMA completion waits are bounded: when one runs out the simulation's
 // flag in `lu_fail` is set, the kernel waits (bounded) for its MMAs still in
 // flight, releases its tensor memory and stops; the solver then reports the
@@ -34,20 +36,41 @@ constexpr uint32_t kTmemCols = 2 * kTile;
 constexpr int kOpBytes = kTile * 64;  // one 128-row, 32-wide-K BF16 operand tile (hi or lo)
 
 // Shared memory of one CTA for half bandwidth b (bytes): mbarriers and the tensor-memory slot,
-// the FP32 panel ((32 + b) x 32, odd column stride), the B operand (hi and lo, q <= b columns
-// rounded up to 128) and one A operand chunk (hi and lo).
+// the FP32 panel ((32 + b) x 32, odd column stride), the B operand (three parts, q <= b columns
+// rounded up to 128) and one A operand chunk (three parts).
 __host__ __device__ inline size_t tc_ldp(int b) { return (size_t)kPanel + b; }
 __host__ __device__ inline size_t tc_npad(int b) { return ((size_t)b + kTile - 1) / kTile * kTile; }
 __host__ __device__ inline size_t tc_smem_bytes(int b) {
-  return 1024 + sizeof(float) * tc_ldp(b) * kPanel + 2 * 64 * tc_npad(b) + 2 * (size_t)kOpBytes;
+  return 1024 + sizeof(float) * tc_ldp(b) * kPanel + 3 * 64 * tc_npad(b) + 3 * (size_t)kOpBytes;
 }
 
+// Eight consecutive K values of one operand row, split into parts, stored at `off` of each part.
 __device__ __forceinline__ void store_pair(char* hi, char* lo, uint32_t off, const float (&x)[8]) {
   __nv_bfloat16 h[8], l[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) umma::split_bf16(x[j], h[j], l[j]);
   *reinterpret_cast<uint4*>(hi + off) = *reinterpret_cast<const uint4*>(h);
   *reinterpret_cast<uint4*>(lo + off) = *reinterpret_cast<const uint4*>(l);
+}
+__device__ __forceinline__ void store_triple(char* const (&part)[3], uint32_t off, const float (&x)[8]) {
+  __nv_bfloat16 h[8], m[8], l[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) umma::split3_bf16(x[j], h[j], m[j], l[j]);
+  *reinterpret_cast<uint4*>(part[0] + off) = *reinterpret_cast<const uint4*>(h);
+  *reinterpret_cast<uint4*>(part[1] + off) = *reinterpret_cast<const uint4*>(m);
+  *reinterpret_cast<uint4*>(part[2] + off) = *reinterpret_cast<const uint4*>(l);
+}
+
+// The six products of two three-part splits above FP32's rounding level, smallest first, for
+// one K step (byte offset ko into every part); the first accumulates onto D only if acc.
+__device__ __forceinline__ void mma_split3(uint32_t dt, const uint32_t (&a)[3], const uint32_t (&b)[3], uint32_t ko,
+                                           uint32_t idesc, uint32_t acc) {
+  constexpr int pa[6] = {1, 2, 0, 1, 0, 0};  // A part: mid, lo, hi, mid, hi, hi
+  constexpr int pb[6] = {1, 0, 2, 0, 1, 0};  // B part: mid, hi, lo, hi, mid, hi
+#pragma unroll
+  for (int t = 0; t < 6; ++t)
+    umma::mma_bf16(dt, umma::smem_desc(a[pa[t]] + ko, 128, 512), umma::smem_desc(b[pb[t]] + ko, 128, 512), idesc,
+                   t == 0 ? acc : 1u);
 }
 
 }  // namespace
@@ -68,11 +91,12 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
   int* sfail = reinterpret_cast<int*>(smc + 128);
   const int ldp = (int)tc_ldp(b);
   float* P = reinterpret_cast<float*>(smc + 1024);                        // panel, ldp x 32 column-major
-  char* Bhi = reinterpret_cast<char*>(P + (size_t)ldp * kPanel);          // B operand: q columns (N), K = 32
   const size_t npad = tc_npad(b);
-  char* Blo = Bhi + 64 * npad;
-  char* Ahi = Blo + 64 * npad;                                            // A operand chunk: 128 rows (M)
-  char* Alo = Ahi + kOpBytes;
+  char* const Bp[3] = {reinterpret_cast<char*>(P + (size_t)ldp * kPanel),  // B operand: q columns (N), K = 32
+                       reinterpret_cast<char*>(P + (size_t)ldp * kPanel) + 64 * npad,
+                       reinterpret_cast<char*>(P + (size_t)ldp * kPanel) + 128 * npad};
+  char* const Ap[3] = {Bp[2] + 64 * npad, Bp[2] + 64 * npad + kOpBytes,  // A operand chunk: 128 rows (M)
+                       Bp[2] + 64 * npad + 2 * kOpBytes};
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int nw = kTcThreads / 32;
 
@@ -136,14 +160,14 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         float x[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[j] = col[8 * g + j];
-        store_pair(Bhi, Blo, umma::kmajor_offset(c, 8 * g), x);
+        store_triple(Bp, umma::kmajor_offset(c, 8 * g), x);
       }
     }
     // B columns past q (up to the 128-column tile) are zero
     for (int c = q + threadIdx.x; c < (int)((q + kTile - 1) / kTile * kTile); c += kTcThreads) {
       const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int g = 0; g < 4; ++g) store_pair(Bhi, Blo, umma::kmajor_offset(c, 8 * g), z);
+      for (int g = 0; g < 4; ++g) store_triple(Bp, umma::kmajor_offset(c, 8 * g), z);
     }
     // ---- 3. inverses of L11 (unit lower) and U11 (upper), as k_band_lu
     if (warp == 0) {
@@ -188,7 +212,7 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         float x[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[j] = m < q ? P[(kPanel + m) + ldp * (8 * g + j)] : 0.f;
-        store_pair(Ahi, Alo, umma::kmajor_offset(ml, 8 * g), x);
+        store_triple(Ap, umma::kmajor_offset(ml, 8 * g), x);
       }
       umma::fence_proxy_async();  // operand writes visible to the tensor core
       umma::fence_before_sync();
@@ -197,16 +221,12 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
       // tile (mc, nc) accumulates in tensor-memory columns 128 (nc % 2) ..
       auto issue = [&](int nc) {
         const uint32_t dt = tmem + (uint32_t)(kTile * (nc & 1));
-        const uint32_t a_hi = umma::smem_addr(Ahi), a_lo = umma::smem_addr(Alo);
-        const uint32_t b_hi = umma::smem_addr(Bhi + (size_t)nc * kOpBytes);
-        const uint32_t b_lo = umma::smem_addr(Blo + (size_t)nc * kOpBytes);
+        const uint32_t a[3] = {umma::smem_addr(Ap[0]), umma::smem_addr(Ap[1]), umma::smem_addr(Ap[2])};
+        const uint32_t bb[3] = {umma::smem_addr(Bp[0] + (size_t)nc * kOpBytes),
+                                umma::smem_addr(Bp[1] + (size_t)nc * kOpBytes),
+                                umma::smem_addr(Bp[2] + (size_t)nc * kOpBytes)};
 #pragma unroll
-        for (int ks = 0; ks < 2; ++ks) {  // K = 32 as two MMAs of K = 16
-          const uint32_t o = 256u * ks;
-          umma::mma_bf16(dt, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_hi + o, 128, 512), idesc, ks);
-          umma::mma_bf16(dt, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_lo + o, 128, 512), idesc, 1);
-          umma::mma_bf16(dt, umma::smem_desc(a_lo + o, 128, 512), umma::smem_desc(b_hi + o, 128, 512), idesc, 1);
-        }
+        for (int ks = 0; ks < 2; ++ks) mma_split3(dt, a, bb, 256u * ks, idesc, ks);  // K = 32 as two K = 16 steps
         umma::commit(&bar[nc & 1]);
         pending[nc & 1] += 1;
       };
@@ -289,24 +309,28 @@ __global__ void k_umma_selftest(const float* __restrict__ A, const float* __rest
   extern __shared__ __align__(1024) char smc[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smc);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smc + 64);
-  char* Ahi = smc + 1024;
-  char* Alo = Ahi + kOpBytes;
-  char* Bhi = Alo + kOpBytes;
-  char* Blo = Bhi + 2 * kOpBytes;  // N <= 256 rows
+  char* const Ap[3] = {smc + 1024, smc + 1024 + kOpBytes, smc + 1024 + 2 * kOpBytes};
+  char* const Bp[3] = {Ap[2] + kOpBytes, Ap[2] + 3 * kOpBytes, Ap[2] + 5 * kOpBytes};  // N <= 256 rows each
+  char* Ahi = Ap[0];
+  char* Alo = Ap[1];
+  char* Bhi = Bp[0];
+  char* Blo = Bp[1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int u = threadIdx.x; u < kTile * 4; u += blockDim.x) {
     const int r = u % kTile, g = u / kTile;
     float x[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) x[j] = A[r * 32 + 8 * g + j];
-    store_pair(Ahi, Alo, umma::kmajor_offset(r, 8 * g), x);
+    if (split == 2) store_triple(Ap, umma::kmajor_offset(r, 8 * g), x);
+    else store_pair(Ahi, Alo, umma::kmajor_offset(r, 8 * g), x);
   }
   for (int u = threadIdx.x; u < N * 4; u += blockDim.x) {
     const int r = u % N, g = u / N;
     float x[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) x[j] = Bm[r * 32 + 8 * g + j];
-    store_pair(Bhi, Blo, umma::kmajor_offset(r, 8 * g), x);
+    if (split == 2) store_triple(Bp, umma::kmajor_offset(r, 8 * g), x);
+    else store_pair(Bhi, Blo, umma::kmajor_offset(r, 8 * g), x);
   }
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
@@ -322,8 +346,14 @@ __global__ void k_umma_selftest(const float* __restrict__ A, const float* __rest
     const uint32_t idesc = umma::idesc_bf16_f32(kTile, N);
     const uint32_t a_hi = umma::smem_addr(Ahi), a_lo = umma::smem_addr(Alo);
     const uint32_t b_hi = umma::smem_addr(Bhi), b_lo = umma::smem_addr(Blo);
+    const uint32_t a3[3] = {umma::smem_addr(Ap[0]), umma::smem_addr(Ap[1]), umma::smem_addr(Ap[2])};
+    const uint32_t b3[3] = {umma::smem_addr(Bp[0]), umma::smem_addr(Bp[1]), umma::smem_addr(Bp[2])};
     for (int ks = 0; ks < 2; ++ks) {
       const uint32_t o = 256u * ks;
+      if (split == 2) {
+        mma_split3(tmem, a3, b3, o, idesc, ks);
+        continue;
+      }
       umma::mma_bf16(tmem, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_hi + o, 128, 512), idesc, ks);
       if (split) {
         umma::mma_bf16(tmem, umma::smem_desc(a_hi + o, 128, 512), umma::smem_desc(b_lo + o, 128, 512), idesc, 1);
@@ -356,12 +386,12 @@ __global__ void k_umma_selftest(const float* __restrict__ A, const float* __rest
 
 extern "C" int eb_umma_selftest(const float* A, const float* B, int32_t N, int32_t split, float* D) {
   using namespace eb;
-  if (!A || !B || !D || !(N == 64 || N == 128 || N == 256)) return EB_ERR_ARG;
+  if (!A || !B || !D || !(N == 64 || N == 128 || N == 256) || split < 0 || split > 2) return EB_ERR_ARG;
   float *dA = nullptr, *dB = nullptr, *dD = nullptr;
   int* dst = nullptr;
   int st = 0;
   cudaError_t e = cudaSuccess;
-  const size_t smem = 1024 + 2 * (size_t)kOpBytes + 4 * (size_t)kOpBytes;
+  const size_t smem = 1024 + 3 * (size_t)kOpBytes + 6 * (size_t)kOpBytes;
   if ((e = cudaMalloc(&dA, sizeof(float) * 128 * 32)) == cudaSuccess &&
       (e = cudaMalloc(&dB, sizeof(float) * (size_t)N * 32)) == cudaSuccess &&
       (e = cudaMalloc(&dD, sizeof(float) * 128 * (size_t)N)) == cudaSuccess &&

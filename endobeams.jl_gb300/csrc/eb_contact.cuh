@@ -23,7 +23,8 @@ struct SurfaceDev {
   double cx, cy, cz, R;    // sphere
   int axis;                // plane: x[axis] = pos, body on the positive side
   double pos;
-  const double* coef;      // (nx+2)(ny+2)(nz+2) prefiltered coefficients, x fastest
+  const double* coef;      // (nx+2)(ny+2)(nz+2) prefiltered coefficients (interp 1: the samples), x fastest
+  int interp;              // 0 quadratic B-spline (the reference's), 1 trilinear
   int nx, ny, nz;          // grid points
   double x0, y0, z0;       // first grid point
   double ihx, ihy, ihz;    // 1 / spacing
@@ -86,9 +87,54 @@ EB_DEV int bspline_axis(double t, int n, double w[3], double d[3]) {
   return i;
 }
 
+// Cell index (clamped to the grid's n-1 cells) and fraction along one axis.
+EB_DEV int linear_axis(double t, int n, double* f) {
+  int i = (int)floor(t);
+  i = i < 0 ? 0 : (i > n - 2 ? n - 2 : i);
+  *f = t - (double)i;
+  return i;
+}
+
+// Trilinear interpolant of the samples (8 taps of the padded grid, sample (i,j,k) at
+// padded (i+1,j+1,k+1)): value, gradient and Hessian of the interpolating polynomial of
+// the cell (its diagonal second derivatives vanish; the mixed ones do not).
+EB_DEV double sdf_eval_linear(const SurfaceDev& s, V3 x, V3* grad, M3* hess) {
+  double fx, fy, fz;
+  const int ix = linear_axis((x.x - s.x0) * s.ihx, s.nx, &fx);
+  const int iy = linear_axis((x.y - s.y0) * s.ihy, s.ny, &fy);
+  const int iz = linear_axis((x.z - s.z0) * s.ihz, s.nz, &fz);
+  const long px = s.nx + 2, py = s.ny + 2;
+  const double* base = s.coef + ((ix + 1) + px * ((iy + 1) + py * (long)(iz + 1)));
+  const double wx[2] = {1 - fx, fx}, wy[2] = {1 - fy, fy}, wz[2] = {1 - fz, fz};
+  const double dd[2] = {-1.0, 1.0};
+  double v = 0, gx = 0, gy = 0, gz = 0, hxy = 0, hxz = 0, hyz = 0;
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const double* row = base + px * (b + py * c);
+      const double q0 = __ldg(row), q1 = __ldg(row + 1);
+      const double sw = wx[0] * q0 + wx[1] * q1, sd = q1 - q0;
+      v += wy[b] * wz[c] * sw;
+      gx += wy[b] * wz[c] * sd;
+      gy += dd[b] * wz[c] * sw;
+      gz += wy[b] * dd[c] * sw;
+      hxy += dd[b] * wz[c] * sd;
+      hxz += wy[b] * dd[c] * sd;
+      hyz += dd[b] * dd[c] * sw;
+    }
+  if (grad) {
+    *grad = v3(gx * s.ihx, gy * s.ihy, gz * s.ihz);
+    const double exy = hxy * (s.ihx * s.ihy), exz = hxz * (s.ihx * s.ihz), eyz = hyz * (s.ihy * s.ihz);
+    *hess = rows(0.0, exy, exz, exy, 0.0, eyz, exz, eyz, 0.0);
+  }
+  return v;
+}
+
 // Value (and optionally gradient and Hessian) of the scaled quadratic
 // B-spline interpolant at world point x (27 taps of the padded grid).
 EB_DEV double sdf_eval(const SurfaceDev& s, V3 x, V3* grad, M3* hess) {
+  if (s.interp == 1) return sdf_eval_linear(s, x, grad, hess);
   double wx[3], wy[3], wz[3], dx[3], dy[3], dz[3];
   int ix = bspline_axis((x.x - s.x0) * s.ihx, s.nx, wx, dx);
   int iy = bspline_axis((x.y - s.y0) * s.ihy, s.ny, wy, dy);

@@ -144,15 +144,42 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   }
 
   double v1[1] = {0.0};
+  const bool use_x0 = a.x0_on != nullptr && a.x0_on[s] != 0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double bi = fx[i] ? 0.0 : b[i];
-    X[i] = 0.0;
+    X[i] = (use_x0 && !fx[i]) ? a.dD[o + i] : 0.0;
     R[i] = bi;
     v1[0] += bi * bi;
   }
   block_sum<1>(v1, red);
   const double bnorm = sqrt(v1[0]);
   double rnorm = bnorm;
+  if (use_x0 && isfinite(bnorm)) {
+    // initial guess: X = α x0 with α = <A x0, b> / <A x0, A x0> clipped to [0, 1], so that
+    // ‖b − A X‖ <= ‖b‖ (a guess that does not help costs one FP64 product)
+    cta_spmv<double, double, double, double>(a.Kt, a.row_ptr, a.col, n0, n, X, R, fx);
+    __syncthreads();
+    double yb[2] = {0.0, 0.0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double bi = fx[i] ? 0.0 : b[i];
+      yb[0] += R[i] * bi;
+      yb[1] += R[i] * R[i];
+    }
+    block_sum<2>(yb, red);
+    double alpha = yb[1] > 0.0 ? yb[0] / yb[1] : 0.0;
+    if (!(alpha > 0.0)) alpha = 0.0;
+    if (alpha > 1.0) alpha = 1.0;
+    double rr0[1] = {0.0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double bi = fx[i] ? 0.0 : b[i];
+      X[i] *= alpha;
+      const double ri = bi - alpha * R[i];
+      R[i] = ri;
+      rr0[0] += ri * ri;
+    }
+    block_sum<1>(rr0, red);
+    rnorm = sqrt(rr0[0]);
+  }
   int its = 0, refs = 0, status = 0;
   if (!isfinite(bnorm)) status = 2;  // EB_SIM_NAN
   // the tensor-core factorisation of these factors stopped at a bounded wait: not trusted

@@ -43,6 +43,8 @@ struct SolverArgs {
   double forcing_max;
   double* prev_bnorm;    // per sim: right-hand side norm of the previous corrector solve (0: none this step)
   double* prev_eta;      // per sim: its forcing term
+  const int* x0_on;      // per sim (may be null): 1 = dD holds an initial guess x0 for this solve; GMRES
+                         // starts from α x0 with α in [0, 1] minimising ‖b − α A x0‖
 };
 
 void launch_block_jacobi(const Dev& d, double* Dinv64, float* Dinv32, cudaStream_t s);

@@ -73,6 +73,7 @@ struct DBuf {
 
 // defined in eb_abi.cu
 std::vector<double> eb_sdf_coefficients_host(const double* values, const int64_t dims[3], bool negate);
+std::vector<double> eb_sdf_samples_padded_host(const double* values, const int64_t dims[3], bool negate);
 int eb_internal_fail(int code, const char* msg);
 
 namespace {
@@ -113,13 +114,19 @@ extern "C" int eb_contact_eval(int64_t n, const double* in, const double* gauss6
     s.axis = (int)surf[1];
     s.pos = surf[2];
   }
-  if (s.kind < 0 || s.kind > 2 || s.axis < 0 || s.axis > 2) return EB_ERR_ARG;
+  if (s.kind < 0 || s.kind > 3 || s.axis < 0 || s.axis > 2) return EB_ERR_ARG;
+  if (s.kind == 3) {  // voxel SDF, trilinear
+    s.kind = 1;
+    s.interp = 1;
+    if (surf[5] < 2 || surf[6] < 2 || surf[7] < 2) return EB_ERR_ARG;
+  }
   DBuf dcoef, di, dout, dfl;
   cudaError_t e;
   if (s.kind == 1) {
     if (!values) return EB_ERR_ARG;
     int64_t dims[3] = {(int64_t)surf[5], (int64_t)surf[6], (int64_t)surf[7]};
-    std::vector<double> c = eb_sdf_coefficients_host(values, dims, false);
+    std::vector<double> c = s.interp ? eb_sdf_samples_padded_host(values, dims, false)
+                                     : eb_sdf_coefficients_host(values, dims, false);
     if ((e = cudaMalloc(&dcoef.p, sizeof(double) * c.size())) != cudaSuccess) return err("cudaMalloc", e);
     cudaMemcpy(dcoef.p, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice);
     s.coef = (const double*)dcoef.p;

@@ -102,5 +102,15 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
   lo = __float2bfloat16_rn(x - __bfloat162float(hi));
 }
 
+// x split into three BF16 parts whose sum carries FP32's 24 significant bits; a product of two
+// such splits summed over the six terms above 2^-24 (hh, hm, mh, hl, lh, mm) has the rounding
+// error of an FP32 product.
+__device__ __forceinline__ void split3_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  const float r = x - __bfloat162float(hi);
+  mid = __float2bfloat16_rn(r);
+  lo = __float2bfloat16_rn(r - __bfloat162float(mid));
+}
+
 }  // namespace umma
 }  // namespace eb

@@ -82,7 +82,7 @@ typedef struct {
                                              with bulk asynchronous copies (same arithmetic, same results);
                                              2: as 1, but the first block's wait expects 16 bytes that no copy
                                              delivers, so it runs out (tests EB_SIM_WAIT_TIMEOUT) */
-  int32_t warm_start;                     /* EB_WS_OFF | EB_WS_LEARNED (needs eb_ws_set_model) */
+  int32_t warm_start;                     /* EB_WS_OFF | EB_WS_LEARNED | EB_WS_LEARNED_X0 (need eb_ws_set_model) */
   int32_t use_graph;                      /* 1: each Newton iteration is one CUDA graph launch (captured once
                                              per handle and refactorisation variant); not with timing = 1,
                                              whose per-phase events need separate launches */
@@ -98,9 +98,9 @@ typedef struct {
 
 /* Band LU engine */
 #define EB_LU_FP32 0    /* FP32 on the CUDA cores */
-#define EB_LU_TENSOR 1  /* panels in FP32, trailing updates on the tensor cores as sums of three BF16
-                           products (operands split into BF16 pairs, FP32 accumulation); the FP32 engine
-                           where the band is too wide for its shared memory (b > ~800) */
+#define EB_LU_TENSOR 1  /* panels in FP32, trailing updates on the tensor cores: operands split into three
+                           BF16 parts, six BF16 products accumulated in FP32 (an FP32 product's rounding);
+                           the FP32 engine where the band is too wide for its shared memory (b > ~590) */
 
 /* When a simulation's band LU is refactorised (besides missing factors and a changed Δt) */
 #define EB_REFACTOR_THRESHOLD 0  /* a solve needed more than refactor_its GMRES iterations */
@@ -117,6 +117,10 @@ typedef struct {
 
 /* Newton start of each step */
 #define EB_WS_OFF 0      /* HHT predictor (predictor.jl:1-27) */
+#define EB_WS_LEARNED_X0 2  /* the HHT predictor (predictor.jl:1-27) with the per-node MLP increment as the
+                              initial guess of its linear solve (scaled by the α in [0, 1] minimising the
+                              initial residual): the same Newton iterate to the linear tolerance, fewer GMRES
+                              iterations when the guess is good */
 #define EB_WS_LEARNED 1  /* per-node MLP increment; per simulation, the predictor again when the learned
                             start's residual exceeds the predictor's right-hand side; after k rejections
                             in a row a simulation uses the predictor for 2^(k-1) steps (at most 32)
@@ -125,6 +129,12 @@ typedef struct {
 /* GMRES preconditioner */
 #define EB_PRECOND_BAND 0          /* FP32 band LU in reverse Cuthill-McKee order (block-Jacobi where it does not fit) */
 #define EB_PRECOND_BLOCK_JACOBI 1  /* LU of each node's 6x6 diagonal block */
+
+/* Interpolation of a voxel SDF */
+#define EB_SDF_QUADRATIC 0  /* quadratic B-spline of the prefiltered samples, Reflect(OnCell()) ends
+                               (Interpolations.jl as the reference uses it, def_interactions.jl:77) */
+#define EB_SDF_TRILINEAR 1  /* trilinear interpolation of the samples themselves (8 taps, no prefilter;
+                               gradient discontinuous across cell faces); needs >= 2 points per axis */
 
 /* Surface kinds */
 #define EB_SURFACE_NONE 0
@@ -157,6 +167,7 @@ typedef struct {
   double sdf_origin[3], sdf_spacing[3];
   const double *sdf_values;                       /* nx*ny*nz, x fastest (VTK order) */
   int32_t sdf_inside;                             /* 1: use values as given, 0: negate (def_interactions.jl:71) */
+  int32_t sdf_interp;                             /* EB_SDF_QUADRATIC (the reference's) | EB_SDF_TRILINEAR */
   int32_t plane_axis;                             /* PlaneSurface.axis: 0 x, 1 y, 2 z */
   double plane_position;                          /* PlaneSurface.position */
 } eb_sim_desc;
@@ -172,7 +183,7 @@ typedef struct {
   double last_res_norm, last_dD_norm;
   double max_linear_rel_residual;  /* worst FP64 relative residual of the step's linear solves */
   int32_t warm_start_used;         /* 1: the step started from the learned increment */
-  int32_t reserved;
+  int32_t predictor_krylov_iterations; /* GMRES iterations of the step's predictor solve */
   double predictor_rhs_norm;       /* ‖r_free‖ of the HHT predictor's right-hand side (learned mode) */
   double start_res_norm;           /* ‖r_free‖ at the learned start (learned mode) */
 } eb_sim_stats;
@@ -279,7 +290,7 @@ int eb_vtk_close(eb_handle *h);
  * in:  n x 96 packed records (layout in the implementation notes), out: n x 458
  * (strain, kinetic, Tint[12], Tk[12], K[144], M[144], C[144]; 12x12 column-major). */
 int eb_element_eval(int64_t n, const double *in, const double *gauss6, double *out);
-/* Contact: surf = [kind(0 sphere,1 sdf,2 plane), cx, cy, cz, R, nx, ny, nz, x0, y0, z0, hx, hy, hz]
+/* Contact: surf = [kind(0 sphere,1 sdf,2 plane,3 trilinear sdf), cx, cy, cz, R, nx, ny, nz, x0, y0, z0, hx, hy, hz]
  * (plane: [2, axis, position, ...]);
  * values = SDF grid (x fastest) when kind = 1; props = [kn, mu, eps_t, eta_n];
  * out n x 301 (energy, Tc[12], Kc[144], Cc[144]); flags[n] = 1 if any Gauss point touched. */
@@ -315,7 +326,8 @@ int eb_contact_eval_noalloc(int64_t n, const double *d_in, const double *gauss6,
 /* Tensor-core self-test (no reference counterpart): D (128 x N, row-major) = A (128 x 32) Bᵀ
  * (B: N x 32), both row-major FP32, on one CTA with the MMA, operand layout and tensor-memory
  * epilogue of the tensor-core band LU; split = 0 rounds A and B to BF16, split = 1 sums the
- * three BF16 products of their BF16 pairs.  N is 64, 128 or 256. */
+ * three BF16 products of their BF16 pairs, split = 2 the six products of their three-part BF16
+ * splits (the band LU's arithmetic).  N is 64, 128 or 256. */
 int eb_umma_selftest(const float *A, const float *B, int32_t N, int32_t split, float *D);
 
 /* Measured FP64 FMA throughput of device 0 in TFLOP/s (independent FMA

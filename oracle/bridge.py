@@ -41,7 +41,8 @@ def scene_from_conf(conf, inter=None) -> O.Scene:
             sc.surface = dict(kind="plane", axis=m.axis_index, position=float(m.position))
         elif hasattr(m, "values"):
             vals = np.asarray(m.values, float)
-            sc.surface = dict(kind="sdf", field=vals if m.inside else -vals, x0=m.origin, h=m.spacing)
+            sc.surface = dict(kind="sdf", field=vals if m.inside else -vals, x0=m.origin, h=m.spacing,
+                              interp=getattr(m, "interpolation", "quadratic"))
         else:
             sc.surface = dict(kind="sphere", center=np.asarray(m.center, float), radius=float(m.radius))
     return sc

@@ -45,7 +45,8 @@ void compute_beams(const double* in, const Gauss& g, double* out);
 
 // ---- rigid surfaces (src/interactions/*) ----
 struct Surface {
-  int kind;            // 0 = SphereSurface, 1 = DiscreteSignedDistanceField (quadratic B-spline), 2 = PlaneSurface
+  int kind;            // 0 = SphereSurface, 1 = DiscreteSignedDistanceField (quadratic B-spline), 2 = PlaneSurface,
+                       // 3 = voxel SDF interpolated trilinearly (coef = the padded samples, no prefilter)
   double center[3];    // sphere
   double radius;       // sphere
   int axis;            // plane: 0 x, 1 y, 2 z (PlaneSurface.axis)

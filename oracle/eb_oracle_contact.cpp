@@ -123,7 +123,56 @@ static void bweights(double t, int64_t n, int64_t* ix, double w[3], double d[3],
   dd[2] = 1.0;
 }
 
+// Trilinear interpolation of the samples (surface kind 3; sample (i,j,k) at padded (i+1,j+1,k+1)):
+// in the cell [i, i+1] x [j, j+1] x [k, k+1] that holds x (cells clamped to the grid), the
+// polynomial Σ w_a(fx) w_b(fy) w_c(fz) q_abc with w_0(f) = 1 - f, w_1(f) = f; its gradient and
+// Hessian are those of the polynomial (∂²/∂x² = 0, mixed second derivatives from w' = ∓1).
+static void sdf_eval_trilinear(const Surface& s, const V3& x, double* val, V3* grad, M3* hess) {
+  int64_t n[3] = {s.nx, s.ny, s.nz};
+  int64_t ix[3];
+  double w[3][2], d[3][2];
+  for (int a = 0; a < 3; ++a) {
+    double t = (x[a] - s.x0[a]) / s.h[a];
+    int64_t i = (int64_t)std::floor(t);
+    if (i < 0) i = 0;
+    if (i > n[a] - 2) i = n[a] - 2;
+    double f = t - (double)i;
+    ix[a] = i + 1;
+    w[a][0] = 1 - f;
+    w[a][1] = f;
+    d[a][0] = -1.0;
+    d[a][1] = 1.0;
+  }
+  const int64_t px = s.nx + 2, py = s.ny + 2;
+  double v = 0, g[3] = {0, 0, 0}, H01 = 0, H02 = 0, H12 = 0;
+  for (int c = 0; c < 2; ++c)
+    for (int b = 0; b < 2; ++b)
+      for (int a = 0; a < 2; ++a) {
+        double q = s.coef[(ix[0] + a) + px * ((ix[1] + b) + py * (ix[2] + c))];
+        v += w[0][a] * w[1][b] * w[2][c] * q;
+        g[0] += d[0][a] * w[1][b] * w[2][c] * q;
+        g[1] += w[0][a] * d[1][b] * w[2][c] * q;
+        g[2] += w[0][a] * w[1][b] * d[2][c] * q;
+        H01 += d[0][a] * d[1][b] * w[2][c] * q;
+        H02 += d[0][a] * w[1][b] * d[2][c] * q;
+        H12 += w[0][a] * d[1][b] * d[2][c] * q;
+      }
+  *val = v;
+  if (grad) *grad = v3(g[0] / s.h[0], g[1] / s.h[1], g[2] / s.h[2]);
+  if (hess) {
+    M3 h = zm3();
+    h(0, 1) = h(1, 0) = H01 / (s.h[0] * s.h[1]);
+    h(0, 2) = h(2, 0) = H02 / (s.h[0] * s.h[2]);
+    h(1, 2) = h(2, 1) = H12 / (s.h[1] * s.h[2]);
+    *hess = h;
+  }
+}
+
 void sdf_eval(const Surface& s, const V3& x, double* val, V3* grad, M3* hess) {
+  if (s.kind == 3) {
+    sdf_eval_trilinear(s, x, val, grad, hess);
+    return;
+  }
   int64_t n[3] = {s.nx, s.ny, s.nz};
   int64_t ix[3];
   double w[3][3], d[3][3], dd[3][3];

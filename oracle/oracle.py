@@ -217,7 +217,7 @@ class Scene:
     loaded_dofs: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     force_fn: Optional[Callable[[float, int], float]] = None  # (t, 1-based dof)
     contact_props: Optional[tuple] = None  # (kn, mu, eps_t, eta_n)
-    surface: Optional[dict] = None  # {"kind": "sphere", center, radius} | {"kind": "sdf", field, x0, h}
+    surface: Optional[dict] = None  # {"kind": "sphere", center, radius} | {"kind": "sdf", field, x0, h, interp}
     #                                | {"kind": "plane", axis (0..2), position}
     contact_elems: Optional[np.ndarray] = None
 
@@ -240,11 +240,16 @@ def surface_arrays(surface: Optional[dict]):
     else:
         field = np.asarray(surface["field"], float)
         nz, ny, nx = field.shape
-        s[0] = 1
+        s[0] = 3 if surface.get("interp") == "trilinear" else 1
         s[5:8] = (nx, ny, nz)
         s[8:11] = surface["x0"]
         s[11:14] = surface["h"]
-        coef = sdf_prefilter(field)
+        if s[0] == 3:  # the samples themselves, in the padded layout (sample (i,j,k) at (i+1,j+1,k+1))
+            coef = np.zeros((nz + 2, ny + 2, nx + 2))
+            coef[1:-1, 1:-1, 1:-1] = field
+            coef = coef.ravel()
+        else:
+            coef = sdf_prefilter(field)
     return s, coef
 
 

@@ -67,3 +67,32 @@ extern "C" void host_contact_eval(int64_t n, const double* in, const double* gau
     contact_element(c, g, cp, s, co, &any);
   }
 }
+
+// Voxel-SDF surfaces: surf[0] = 1 (quadratic B-spline, coef = prefiltered coefficients) or
+// 3 (trilinear, coef = the samples), both in the padded (nx+2)(ny+2)(nz+2) layout.
+extern "C" void host_contact_eval_grid(int64_t n, const double* in, const double* gauss6, const double* props,
+                                       const double* surf, const double* coef, double* out) {
+  const Gauss3 g = gauss(gauss6);
+  const ContactProps cp{props[0], props[1], props[2], props[3]};
+  SurfaceDev s{};
+  s.kind = 1;
+  s.interp = surf[0] == 3 ? 1 : 0;
+  s.coef = coef;
+  s.nx = (int)surf[5]; s.ny = (int)surf[6]; s.nz = (int)surf[7];
+  s.x0 = surf[8]; s.y0 = surf[9]; s.z0 = surf[10];
+  s.ihx = 1.0 / surf[11]; s.ihy = 1.0 / surf[12]; s.ihz = 1.0 / surf[13];
+  s.xl = (s.nx - 1) * surf[11]; s.yl = (s.ny - 1) * surf[12]; s.zl = (s.nz - 1) * surf[13];
+  for (int64_t e = 0; e < n; ++e) {
+    const double* p = in + 96 * e;
+    double* o = out + 301 * e;
+    for (int k = 0; k < 301; ++k) o[k] = 0.0;
+    ContactIn c;
+    c.X1 = P3(p + 0); c.X2 = P3(p + 3); c.u1 = P3(p + 6); c.u2 = P3(p + 9);
+    c.R1 = P9(p + 12); c.R2 = P9(p + 21); c.dR1 = P9(p + 30); c.dR2 = P9(p + 39);
+    c.ud1 = P3(p + 48); c.ud2 = P3(p + 51); c.wd1 = P3(p + 54); c.wd2 = P3(p + 57);
+    c.l0 = p[72]; c.Re0 = P9(p + 73); c.radius = p[94];
+    ContactOut co{o + 13, o + 157, o + 1, o + 0};
+    bool any = false;
+    contact_element(c, g, cp, s, co, &any);
+  }
+}

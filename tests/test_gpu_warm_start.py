@@ -97,3 +97,52 @@ def test_committed_stent_model_runs_and_matches_plain(eb, scenes):
     plain = _run(eb, mk, 6, "off")
     learned = _run(eb, mk, 6, "learned", model)
     assert float(np.abs(plain["u"] - learned["u"]).max()) <= 1e-6 * 8e-3
+
+
+def _run_x0(eb, mk, steps, mode, model=None):
+    """Steps with per-step statistics: Newton iterations and the predictor solve's GMRES iterations."""
+    conf, p, inter = mk()
+    p.warm_start = mode
+    eng = eb.GpuSimulations([conf], p, [inter])
+    if model is not None:
+        eng.set_warm_start(model)
+    dt = np.full(1, p.initial_timestep)
+    ks, pred, total = [], [], 0
+    for _ in range(steps):
+        k, status = eng.step(dt)
+        st = eng.stats()[0]
+        assert k[0] <= p.max_iterations and status[0] == 0
+        ks.append(int(k[0]))
+        pred.append(st["predictor_krylov_iterations"])
+        total += st["krylov_iterations"]
+        eng.commit(np.ones(1, np.int32))
+    out = {"ks": np.array(ks), "pred": np.array(pred), "krylov": total, "u": eng.state(0)["u"]}
+    eng.close()
+    return out
+
+
+def test_learned_initial_guess_gain_on_held_out_stents(eb, scenes):
+    """The committed stent model (trained on a seed-7 population) as the initial guess of the HHT
+    predictor's GMRES solve, on stents it has not seen: the Newton iterates are the plain ones to
+    the linear tolerance (same Newton counts, positions within 1e-6 of the stent size) and the
+    predictor solves take fewer GMRES iterations in total."""
+    import os
+    from endobeams_gb300 import warm_start as W
+    path = os.path.join(os.path.dirname(eb.__file__), "models", "warm_start_stents.npz")
+    model = W.WarmStartModel.load(path)
+    gains = []
+    for wires, epw, R in ((16, 80, 3.5e-3), (24, 60, 4.5e-3)):
+        def mk():
+            c, p, it = scenes.braided_stent(wires=wires, elems_per_wire=epw, R=R, cyl_radius=0.9 * R, grid=None)
+            p.krylov_restart = 32
+            p.tolerance_residual = 1e-8
+            p.linear_tol = 1e-4
+            p.precision = "mixed"
+            return c, p, it
+        plain = _run_x0(eb, mk, 12, "off")
+        x0 = _run_x0(eb, mk, 12, "learned_x0", model)
+        assert np.array_equal(plain["ks"], x0["ks"])
+        assert float(np.abs(plain["u"] - x0["u"]).max()) <= 1e-6 * 0.02
+        gains.append((int(plain["pred"][1:].sum()), int(x0["pred"][1:].sum()), plain["krylov"], x0["krylov"]))
+    print("learned initial guess (predictor GMRES its plain -> x0, all GMRES its plain -> x0):", gains)
+    assert sum(g[1] for g in gains) < sum(g[0] for g in gains)
