@@ -14,10 +14,11 @@ Workloads (synthetic, seeded; no dataset):
             (radius U[0.85,0.95] of the stent's, 0.1 mm grid sized to the stent);
             mu = 0.1, dt = 1e-5 s, FP32 GMRES inside FP64 refinement.  The
             population runs as resident groups sized to the device memory;
-            the learned warm start (committed model) is on.  The line also
-            carries the same first group with the plain HHT predictor and the
-            plain single-stent path (48 wires, R = 4 mm, 45 deg, 200 elements
-            per wire, cylinder 3.5 mm) on the same GPU.
+            the learned warm start (committed model) gives the initial guess
+            of each predictor solve.  The line also carries the same groups
+            and step window with the plain HHT predictor, and the plain
+            single-stent path (48 wires, R = 4 mm, 45 deg, 200 elements per
+            wire, cylinder 3.5 mm) on the same GPU.
   stent   — the single 48-wire stent above.
   nets256 — 256 square nets, sides U{20..40} (seed 0), 1 mm spacing, xy jitter
             U(±0.5 mm), r = 0.1 mm, E = 100 GPa, gravity, dropped on a sphere
@@ -84,7 +85,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="stents1024")
     ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
-    ap.add_argument("--warm-start", default=None, choices=[None, "off", "learned"])
+    ap.add_argument("--warm-start", default=None, choices=[None, "off", "learned", "learned_x0"])
     ap.add_argument("--count", type=int, default=None, help="population size override (stents)")
     ap.add_argument("--band-lu", default="fp32", choices=["fp32", "tensor"],
                     help="band LU engine of the stents' preconditioner")
@@ -195,7 +196,7 @@ class Workload:
                 raise SystemExit(f"unknown workload {name}")
             self.count = len(self.variants)
             self.precision = precision or "mixed"
-            self.warm = warm or ("learned" if (name.startswith("stents") and os.path.exists(MODEL)) else "off")
+            self.warm = warm or ("learned_x0" if (name.startswith("stents") and os.path.exists(MODEL)) else "off")
         self.tol_res = {}  # per simulation index: its residual tolerance (stents)
 
     def stats(self, i):
@@ -356,6 +357,7 @@ class Driver:
         self.ok_steps = 0
         self.newton = 0
         self.krylov = 0
+        self.pred_krylov = 0
         self.batch_iters = 0
         self.ws_used = 0
         self.ws_steps = 0
@@ -370,6 +372,7 @@ class Driver:
         self.newton += sum(s["newton_iterations"] for s in st)
         self.batch_iters += max(s["newton_iterations"] for s in st)
         self.krylov += sum(s["krylov_iterations"] for s in st)
+        self.pred_krylov += sum(s["predictor_krylov_iterations"] for s in st)
         # element evaluations of the corrector iterations (one k_beam pass per iteration of each sim)
         self.elem_evals += int(sum(int(e) * s["newton_iterations"] for e, s in zip(self.elems, st)))
         self.ws_used += sum(s["warm_start_used"] for s in st)
@@ -387,8 +390,14 @@ class Driver:
         return k
 
 
-def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
-    """Creates one resident group, warms up, times args.steps steps; returns a dict of totals."""
+def run_group(eb, wl, idx, args, world, e2e=True, warm=None):
+    """Creates one resident group, warms up W steps, times K steps; returns a dict of totals.
+
+    Every timed step goes through the public API with host buffers: the step's loads are
+    uploaded from host memory (eb_set_loads_all) and all displacements are read back
+    (eb_get_displacements).  The same K steps give both figures: the device time between
+    CUDA events on the handle's stream (`ms`, the whole-job HHT steps/s) and the host wall
+    clock around them (`e2e`)."""
     built = [wl.build(i) for i in idx]
     confs = [b[0] for b in built]
     inters = [b[2] for b in built]
@@ -399,47 +408,42 @@ def run_group(eb, wl, idx, args, world, timed=True, e2e=True, warm=None):
     eng = eb.GpuSimulations(confs, params, inters)
     if wl.kind == "stents":
         eng.set_tolerances(residual=[wl.tol_res[i] for i in idx])
-    if params.warm_start == "learned":
+    if params.warm_start in ("learned", "learned_x0"):
         from endobeams_gb300 import warm_start as W
         eng.set_warm_start(W.WarmStartModel.load(MODEL))
     mem, band_sims = eng.memory()
     drv = Driver(eng, params, [len(c.beams) for c in confs])
+    total_nodes = sum(len(c.nodes) for c in confs)
+    ubuf = np.zeros((total_nodes, 3))
+    use_e2e = e2e and not args.no_e2e
     for _ in range(args.warmup):
-        drv.step()
+        drv.step(e2e=use_e2e, ubuf=ubuf)
     launch_shapes = eng.autotune()
     eng.phase_times(reset=True)
     drv.reset()
     barrier(world)
     eng.timer_start()
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        drv.step()
+        drv.step(e2e=use_e2e, ubuf=ubuf)
     ms = allreduce_max(eng.timer_stop(), world)
+    wall = allreduce_max(time.perf_counter() - t0, world)
     phase_ms, launches = eng.phase_times(reset=True)
     out = {"sim_steps": drv.ok_steps, "ms": ms, "newton": drv.newton, "krylov": drv.krylov,
+           "pred_krylov": drv.pred_krylov,
            "ws_used": drv.ws_used, "ws_steps": drv.ws_steps, "phase_ms": phase_ms, "launches": launches,
-           "elem_evals": drv.elem_evals,
-           "nodes": sum(len(c.nodes) for c in confs), "elements": sum(len(c.beams) for c in confs),
+           "elem_evals": drv.elem_evals, "nodes": total_nodes, "elements": sum(len(c.beams) for c in confs),
            "sims": len(idx), "device_bytes": mem, "band_sims": band_sims, "e2e": None,
            "launch_shapes": launch_shapes}
-    if e2e and not args.no_e2e:
-        total_nodes = out["nodes"]
-        ubuf = np.zeros((total_nodes, 3))
+    if use_e2e:
         n_loaded = sum(len(c.loads.concentrated_force.loaded_dofs) for c in confs if c.loads is not None)
-        drv.reset()
-        barrier(world)
-        eng.timer_start()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            drv.step(e2e=True, ubuf=ubuf)
-        wall = allreduce_max(time.perf_counter() - t0, world)
-        dev_ms = eng.timer_stop()
         S = drv.S
         bi = drv.batch_iters / max(args.steps, 1)
         # loads, per-sim step constants (cK, cC, cM, dt), active masks (step + each iteration), commit mask
         h2d = 8 * n_loaded + 32 * S + 4 * S + 4 * S * bi + 4 * S
         # displacements, per-iteration Newton norms, per-step solver statistics
         d2h = 24 * total_nodes + 40 * S * bi + 20 * S
-        out["e2e"] = {"sim_steps": drv.ok_steps, "wall_s": wall, "h2d": h2d, "d2h": d2h, "device_ms": dev_ms,
+        out["e2e"] = {"sim_steps": drv.ok_steps, "wall_s": wall, "h2d": h2d, "d2h": d2h, "device_ms": ms,
                       "newton": drv.newton, "krylov": drv.krylov}
     eng.close()
     return out
@@ -527,8 +531,8 @@ def gpu_arm(args, rank, world):
             tot["launches"] = dict(r["launches"])
             tot["device_bytes_max"] = r["device_bytes"]
         else:
-            for k in ("sim_steps", "ms", "newton", "krylov", "ws_used", "ws_steps", "nodes", "elements", "sims",
-                      "band_sims", "elem_evals"):
+            for k in ("sim_steps", "ms", "newton", "krylov", "pred_krylov", "ws_used", "ws_steps", "nodes", "elements",
+                      "sims", "band_sims", "elem_evals"):
                 tot[k] += r[k]
             tot["device_bytes_max"] = max(tot["device_bytes_max"], r["device_bytes"])
             for k in tot["phase_ms"]:
@@ -545,10 +549,8 @@ def gpu_arm(args, rank, world):
         e = tot["e2e"]
         e2e = {"value": world * e["sim_steps"] / e["wall_s"], "unit": "HHT steps/s",
                "h2d_bytes_per_step": int(e["h2d"] / max(steps, 1)), "d2h_bytes_per_step": int(e["d2h"] / max(steps, 1)),
-               "device_value": world * e["sim_steps"] / (e["device_ms"] / 1e3),
-               # the e2e leg runs the 3 steps after the timed ones; their solver work explains the rate
-               "newton_iters_per_step": e["newton"] / max(e["sim_steps"], 1),
-               "krylov_iters_per_newton": e["krylov"] / max(e["newton"], 1)}
+               "note": "the timed steps themselves: loads uploaded from host memory and all displacements "
+                       "read back every step, host wall clock"}
     phase_ms, launches = tot["phase_ms"], tot["launches"]
     dom = max(phase_ms, key=lambda k: phase_ms[k])
     # ---- rooflines: the element kernel (FP64 pipe) and the Krylov kernel (HBM)
@@ -599,20 +601,30 @@ def gpu_arm(args, rank, world):
                        launch_shapes_first_group=tot["launch_shapes"]),
         "newton_iters_per_step": tot["newton"] / max(tot["sim_steps"], 1),
         "krylov_iters_per_newton": tot["krylov"] / max(tot["newton"], 1),
+        "predictor_krylov_iters_per_step": tot["pred_krylov"] / max(tot["sim_steps"], 1),
         "phase_ms": {k: round(v, 3) for k, v in phase_ms.items()}, "dominant_phase": dom,
         "gpu_launches": int(sum(launches.values())),
         "roofline": roof, "rooflines": rooflines, "e2e": e2e, "clocks": clk,
     }
-    if wl.warm == "learned":
-        out["warm_start"] = {"model": os.path.relpath(MODEL, ROOT),
+    if wl.warm in ("learned", "learned_x0"):
+        out["warm_start"] = {"model": os.path.relpath(MODEL, ROOT), "mode": wl.warm,
                              "learned_start_accepted_frac": tot["ws_used"] / max(tot["ws_steps"], 1)}
-    # ---- comparison legs: the first group with the plain predictor, and the plain single stent
+    # ---- comparison legs: the same groups with the plain predictor, and the plain single stent
     if wl.kind == "stents" and wl.count > 1 and not args.no_compare:
-        if wl.warm == "learned":
-            r = run_group(eb, wl, groups[0], args, world, e2e=False, warm="off")
-            out["batched_plain"] = {"value": world * r["sim_steps"] / (r["ms"] / 1e3), "sims": r["sims"],
-                                    "newton_iters_per_step": r["newton"] / max(r["sim_steps"], 1),
-                                    "note": "first resident group, HHT predictor"}
+        if wl.warm in ("learned", "learned_x0"):
+            pl = {"sim_steps": 0, "ms": 0.0, "newton": 0, "krylov": 0, "pred_krylov": 0}
+            for g_idx in groups:
+                r = run_group(eb, wl, g_idx, args, world, e2e=False, warm="off")
+                for k in pl:
+                    pl[k] += r[k]
+            pv = world * pl["sim_steps"] / (pl["ms"] / 1e3)
+            out["batched_plain"] = {"value": pv, "sims": wl.count,
+                                    "newton_iters_per_step": pl["newton"] / max(pl["sim_steps"], 1),
+                                    "krylov_iters_per_newton": pl["krylov"] / max(pl["newton"], 1),
+                                    "predictor_krylov_iters_per_step": pl["pred_krylov"] / max(pl["sim_steps"], 1),
+                                    "note": "the same resident groups and step window, HHT predictor without the "
+                                            "network"}
+            out["learned_vs_plain"] = value / pv
         single = Workload("stent", wl.precision, "off")
         r = run_group(eb, single, [0], args, world, e2e=False)
         sv = world * r["sim_steps"] / (r["ms"] / 1e3)

@@ -67,17 +67,17 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
     const int kb = min(kPanel, n - k0);
     const int hp = min(n - k0, kb + b);
     const int q = min(n - k0 - kb, b);
-    // ---- load panel (column c = lane, rows strided by warps) and U12 (row r = warp.., columns by lane)
-    if (lane < kb)
-      for (int r = warp; r < hp; r += nw) {
-        const int i = k0 + r, j = k0 + lane;
-        P[r + ldp * lane] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
+    // ---- load the panel and U12: warp per column, lanes along the rows (a band column is
+    // contiguous in rows, so each warp access is one 128-byte line; q > 0 implies kb = 32)
+    for (int c = warp; c < kb; c += nw)
+      for (int r = lane; r < hp; r += 32) {
+        const int i = k0 + r, j = k0 + c;
+        P[r + ldp * c] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
       }
-    for (int r = warp; r < kb; r += nw)
-      for (int c = lane; c < q; c += 32) {
-        const int i = k0 + r, j = k0 + kb + c;
-        U[r * b + c] = (j - i <= b) ? V.at(i, j) : 0.f;
-      }
+    for (int c = warp; c < q; c += nw) {
+      const int i = k0 + lane, j = k0 + kb + c;
+      U[lane * b + c] = (j - i <= b) ? V.at(i, j) : 0.f;
+    }
     __syncthreads();
     // ---- 1. panel LU (column c = lane)
     for (int t = 0; t < kb; ++t) {
@@ -184,17 +184,16 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
         for (int a = 0; a < 8; ++a)
           if ((rv >> a) & (cv >> c) & 1u) V.at(k0 + kb + ti + a * R, k0 + kb + tj + c * R) = old[a][c] - acc[a][c];
     }
-    // ---- write back panel and U12
-    if (lane < kb)
-      for (int r = warp; r < hp; r += nw) {
-        const int i = k0 + r, j = k0 + lane;
-        if (i - j <= b && j - i <= b) V.at(i, j) = P[r + ldp * lane];
+    // ---- write back the panel and U12, warp per column as they were loaded
+    for (int c = warp; c < kb; c += nw)
+      for (int r = lane; r < hp; r += 32) {
+        const int i = k0 + r, j = k0 + c;
+        if (i - j <= b && j - i <= b) V.at(i, j) = P[r + ldp * c];
       }
-    for (int r = warp; r < kb; r += nw)
-      for (int c = lane; c < q; c += 32) {
-        const int i = k0 + r, j = k0 + kb + c;
-        if (j - i <= b) V.at(i, j) = U[r * b + c];
-      }
+    for (int c = warp; c < q; c += nw) {
+      const int i = k0 + lane, j = k0 + kb + c;
+      if (j - i <= b) V.at(i, j) = U[lane * b + c];
+    }
     __syncthreads();
   }
 }

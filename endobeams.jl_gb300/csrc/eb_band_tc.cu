@@ -34,6 +34,7 @@ constexpr int kTcThreads = 256;  // 8 warps: warp w updates lanes 32 (w % 4) ..,
 constexpr int kTile = 128;       // M = N = 128 per MMA
 constexpr uint32_t kTmemCols = 2 * kTile;
 constexpr int kOpBytes = kTile * 64;  // one 128-row, 32-wide-K BF16 operand tile (hi or lo)
+constexpr int kU12 = 3 * kOpBytes / (33 * 4);  // U12 columns staged at a time in the A operand buffers (186)
 
 // Shared memory of one CTA for half bandwidth b (bytes): mbarriers and the tensor-memory slot,
 // the FP32 panel ((32 + b) x 32, odd column stride), the B operand (three parts, q <= b columns
@@ -120,11 +121,12 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
     const int kb = min(kPanel, n - k0);
     const int hp = min(n - k0, kb + b);
     const int q = min(n - k0 - kb, b);
-    // ---- load the panel (column c = lane, rows strided by warps)
-    if (lane < kb)
-      for (int r = warp; r < hp; r += nw) {
-        const int i = k0 + r, j = k0 + lane;
-        P[r + ldp * lane] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
+    // ---- load the panel: warp per column, lanes along the rows (a band column is contiguous in
+    // rows, so each warp access is one 128-byte line)
+    for (int c = warp; c < kb; c += nw)
+      for (int r = lane; r < hp; r += 32) {
+        const int i = k0 + r, j = k0 + c;
+        P[r + ldp * c] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
       }
     __syncthreads();
     // ---- 1. panel LU (column c = lane)
@@ -138,30 +140,45 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
       }
       __syncthreads();
     }
-    // ---- 2. U12 = L11⁻¹ A12 (thread per column; q > 0 implies kb = 32), into the band and B
-    for (int c = threadIdx.x; c < q; c += kTcThreads) {
-      // entries of A12 with j - i > b lie outside the band: zero, and not written back
-      const int rlo = max(0, kPanel + c - b);
-      float col[kPanel];
-#pragma unroll
-      for (int r = 0; r < kPanel; ++r) col[r] = r >= rlo ? V.at(k0 + r, k0 + kPanel + c) : 0.f;
-#pragma unroll
-      for (int r = 1; r < kPanel; ++r) {
-        float acc = col[r];
-#pragma unroll
-        for (int t = 0; t < r; ++t) acc -= P[r + ldp * t] * col[t];
-        col[r] = acc;
+    // ---- 2. U12 = L11⁻¹ A12 (q > 0 implies kb = 32), into the band and B, kU12 columns at a
+    // time through the (idle) A operand buffer: each column is loaded and stored by one warp
+    // (32 rows, one 128-byte line), solved by one thread from shared memory (stride 33: no bank
+    // conflicts).  Entries of A12 with j - i > b lie outside the band: zero, not written back.
+    float* S = reinterpret_cast<float*>(Ap[0]);
+    for (int cs = 0; cs < q; cs += kU12) {
+      const int cn = min(kU12, q - cs);
+      for (int c = warp; c < cn; c += nw) {
+        const int j = k0 + kPanel + cs + c, i = k0 + lane;
+        S[lane + 33 * c] = (j - i <= b) ? V.at(i, j) : 0.f;
       }
+      __syncthreads();
+      for (int c = threadIdx.x; c < cn; c += kTcThreads) {
+        float col[kPanel];
 #pragma unroll
-      for (int r = 0; r < kPanel; ++r)
-        if (r >= rlo) V.at(k0 + r, k0 + kPanel + c) = col[r];
+        for (int r = 0; r < kPanel; ++r) col[r] = S[r + 33 * c];
 #pragma unroll
-      for (int g = 0; g < 4; ++g) {
-        float x[8];
+        for (int r = 1; r < kPanel; ++r) {
+          float acc = col[r];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] = col[8 * g + j];
-        store_triple(Bp, umma::kmajor_offset(c, 8 * g), x);
+          for (int t = 0; t < r; ++t) acc -= P[r + ldp * t] * col[t];
+          col[r] = acc;
+        }
+#pragma unroll
+        for (int r = 0; r < kPanel; ++r) S[r + 33 * c] = col[r];
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          float x[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) x[jj] = col[8 * g + jj];
+          store_triple(Bp, umma::kmajor_offset(cs + c, 8 * g), x);
+        }
       }
+      __syncthreads();
+      for (int c = warp; c < cn; c += nw) {
+        const int j = k0 + kPanel + cs + c, i = k0 + lane;
+        if (j - i <= b) V.at(i, j) = S[lane + 33 * c];
+      }
+      __syncthreads();
     }
     // B columns past q (up to the 128-column tile) are zero
     for (int c = q + threadIdx.x; c < (int)((q + kTile - 1) / kTile * kTile); c += kTcThreads) {
@@ -195,11 +212,11 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
 #pragma unroll
       for (int r = 0; r < kPanel; ++r) Uv[lane * kPanel + r] = z[r];
     }
-    // ---- write back the panel (L11, U11, L21)
-    if (lane < kb)
-      for (int r = warp; r < hp; r += nw) {
-        const int i = k0 + r, j = k0 + lane;
-        if (i - j <= b && j - i <= b) V.at(i, j) = P[r + ldp * lane];
+    // ---- write back the panel (L11, U11, L21), warp per column as it was loaded
+    for (int c = warp; c < kb; c += nw)
+      for (int r = lane; r < hp; r += 32) {
+        const int i = k0 + r, j = k0 + c;
+        if (i - j <= b && j - i <= b) V.at(i, j) = P[r + ldp * c];
       }
     __syncthreads();
     if (q <= 0) continue;

