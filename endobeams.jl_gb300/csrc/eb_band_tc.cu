@@ -30,7 +30,7 @@ namespace eb {
 
 namespace {
 
-constexpr int kTcThreads = 256;  // 8 warps: warp w updates lanes 32 (w % 4) .., columns 64 (w / 4) ..
+constexpr int kTcThreads = 512;  // 16 warps: warp w updates tile lanes 32 (w % 4) .., columns 32 (w / 4) ..
 constexpr int kTile = 128;       // M = N = 128 per MMA
 constexpr uint32_t kTmemCols = 2 * kTile;
 constexpr int kOpBytes = kTile * 64;  // one 128-row, 32-wide-K BF16 operand tile (hi or lo)
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         P[r + ldp * c] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
       }
     __syncthreads();
-    // ---- 1. panel LU (column c = lane)
+    // ---- 1. panel LU (column c = lane, rows strided by warps)
     for (int t = 0; t < kb; ++t) {
       const float ip = 1.f / P[t + ldp * t];
       for (int r = t + 1 + threadIdx.x; r < hp; r += kTcThreads) P[r + ldp * t] *= ip;
@@ -262,23 +262,29 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         // the next tile's MMAs run while this one is written back (its accumulator was
         // released by the barrier that ended tile nc - 1)
         if (threadIdx.x == 0 && nc + 1 < nt) issue(nc + 1);
-        const int quarter = warp & 3, half = warp >> 2;
+        const int quarter = warp & 3, group = warp >> 2;
         const int m = kTile * mc + 32 * quarter + lane;
         const int i = k0 + kPanel + m;
-#pragma unroll
-        for (int cb = 0; cb < 2; ++cb) {
-          const int c0 = 64 * half + 32 * cb;
+        {
+          const int c0 = 32 * group;
           float acc[32];
           umma::ld_32cols(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(kTile * buf + c0), acc);
           if (m < q) {
+            // row i, columns jb .. jb + 31: the columns left of the diagonal (j < i) are in the L
+            // part at L + (i - 1) + (b - 1) j, the others in the U part at U + b + i + b j, so
+            // each address is one multiply-add from two row bases
             const int jb = k0 + kPanel + kTile * nc + c0;
             const int cmax = min(32, q - (kTile * nc + c0));
+            const int sp = min(max(i - jb, 0), 32);
+            float* pL = V.L + ((int64_t)i - 1 + (int64_t)(b - 1) * jb);
+            float* pU = V.U + ((int64_t)b + i + (int64_t)b * jb);
             float old[32];
 #pragma unroll
-            for (int c = 0; c < 32; ++c) old[c] = c < cmax ? V.at(i, jb + c) : 0.f;
+            for (int c = 0; c < 32; ++c)
+              old[c] = c < cmax ? (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) : 0.f;
 #pragma unroll
             for (int c = 0; c < 32; ++c)
-              if (c < cmax) V.at(i, jb + c) = old[c] - acc[c];
+              if (c < cmax) (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) = old[c] - acc[c];
           }
         }
         umma::fence_before_sync();
