@@ -263,7 +263,7 @@ def est_bytes(stats):
     b = 6 * w + 5
     blocks = n + 2 * ne
     band = 4 * (6 * n) * (2 * b + 1) if b <= 891 else 0
-    per_dof = 14 * 8 + 1 + 16 + (m + 1) * 8 + 8 + 4 + 256
+    per_dof = 14 * 8 + 1 + 16 + (2 * m + 1) * 8 + 8 + 4 + 256  # ... Krylov basis V and its preconditioned Z
     return 6300 * ne + 2200 * blocks + 1100 * n + per_dof * 6 * n + band + 8 * pts
 
 

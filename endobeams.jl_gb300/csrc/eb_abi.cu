@@ -1086,13 +1086,14 @@ int eb_create(const eb_params* p, int32_t n_sims, const eb_sim_desc* sims, eb_ha
   sa.Tk1 = d.Tk1;
   CK(A.alloc(&sa.X, ND));
   CK(A.alloc(&sa.R64, ND));
+  // Krylov basis V (m + 1 vectors) and the preconditioned basis Z (m vectors) of every simulation
   if (fp32) {
     float *V, *Z;
-    CK(A.alloc(&V, (size_t)(m + 1) * ND)); CK(A.alloc(&Z, ND));
+    CK(A.alloc(&V, (size_t)(m + 1) * ND)); CK(A.alloc(&Z, (size_t)m * ND));
     sa.V = V; sa.Z = Z;
   } else {
     double *V, *Z;
-    CK(A.alloc(&V, (size_t)(m + 1) * ND)); CK(A.alloc(&Z, ND));
+    CK(A.alloc(&V, (size_t)(m + 1) * ND)); CK(A.alloc(&Z, (size_t)m * ND));
     sa.V = V; sa.Z = Z;
   }
   sa.m = m;

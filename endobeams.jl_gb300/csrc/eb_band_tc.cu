@@ -248,8 +248,25 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         pending[nc & 1] += 1;
       };
       if (threadIdx.x == 0) issue(0);
+      const int quarter = warp & 3, group = warp >> 2;
+      const int m = kTile * mc + 32 * quarter + lane;
+      const int i = k0 + kPanel + m;
       for (int nc = 0; nc < nt; ++nc) {
         const int buf = nc & 1;
+        // row i, columns jb .. jb + 31 of this warp's part of tile nc: the columns left of the
+        // diagonal (j < i) are in the L part at L + (i - 1) + (b - 1) j, the others in the U part
+        // at U + b + i + b j, so each address is one multiply-add from two row bases.  The old
+        // values are loaded before the MMA wait: their latency overlaps the tensor-core work.
+        const int c0 = 32 * group;
+        const int jb = k0 + kPanel + kTile * nc + c0;
+        const int cmax = m < q ? min(32, q - (kTile * nc + c0)) : 0;
+        const int sp = min(max(i - jb, 0), 32);
+        float* pL = V.L + ((int64_t)i - 1 + (int64_t)(b - 1) * jb);
+        float* pU = V.U + ((int64_t)b + i + (int64_t)b * jb);
+        float old[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          old[c] = c < cmax ? (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) : 0.f;
         if (!mbar_wait(&bar[buf], phase[buf])) *sfail = 1;
         if (threadIdx.x == 0 && !*sfail) pending[buf] -= 1;
         phase[buf] ^= 1u;
@@ -262,31 +279,11 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         // the next tile's MMAs run while this one is written back (its accumulator was
         // released by the barrier that ended tile nc - 1)
         if (threadIdx.x == 0 && nc + 1 < nt) issue(nc + 1);
-        const int quarter = warp & 3, group = warp >> 2;
-        const int m = kTile * mc + 32 * quarter + lane;
-        const int i = k0 + kPanel + m;
-        {
-          const int c0 = 32 * group;
-          float acc[32];
-          umma::ld_32cols(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(kTile * buf + c0), acc);
-          if (m < q) {
-            // row i, columns jb .. jb + 31: the columns left of the diagonal (j < i) are in the L
-            // part at L + (i - 1) + (b - 1) j, the others in the U part at U + b + i + b j, so
-            // each address is one multiply-add from two row bases
-            const int jb = k0 + kPanel + kTile * nc + c0;
-            const int cmax = min(32, q - (kTile * nc + c0));
-            const int sp = min(max(i - jb, 0), 32);
-            float* pL = V.L + ((int64_t)i - 1 + (int64_t)(b - 1) * jb);
-            float* pU = V.U + ((int64_t)b + i + (int64_t)b * jb);
-            float old[32];
+        float acc[32];
+        umma::ld_32cols(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(kTile * buf + c0), acc);
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
-              old[c] = c < cmax ? (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) : 0.f;
-#pragma unroll
-            for (int c = 0; c < 32; ++c)
-              if (c < cmax) (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) = old[c] - acc[c];
-          }
-        }
+        for (int c = 0; c < 32; ++c)
+          if (c < cmax) (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) = old[c] - acc[c];
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();

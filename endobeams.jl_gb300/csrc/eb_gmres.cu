@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   double* y = g + m + 1;           // m
   double* red = y + m;             // 8 x 32
   T* V = reinterpret_cast<T*>(a.V) + (int64_t)(m + 1) * o;
-  T* Z = reinterpret_cast<T*>(a.Z) + o;
+  T* Zb = reinterpret_cast<T*>(a.Z) + (int64_t)m * o;  // z_j = M⁻¹ v_j at Zb + j n
   double* X = a.X + o;
   double* R = a.R64 + o;
   const double* b = a.b + o;
@@ -218,10 +218,11 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
       for (int j = 0; j < jmax; ++j) {
         T* vj = V + (int64_t)j * n;
         T* w = V + (int64_t)(j + 1) * n;
-        if (use_band) band_solve<T, T>(a.band, s, n0, n, vj, Z, xs, stp, ph);
-        else cta_prec<T, T, T>(Dm, n0, n, vj, Z);
+        T* zj = Zb + (int64_t)j * n;
+        if (use_band) band_solve<T, T>(a.band, s, n0, n, vj, zj, xs, stp, ph);
+        else cta_prec<T, T, T>(Dm, n0, n, vj, zj);
         __syncthreads();
-        cta_spmv<T, T, T, TACC>(Am, a.row_ptr, a.col, n0, n, Z, w, fx);
+        cta_spmv<T, T, T, TACC>(Am, a.row_ptr, a.col, n0, n, zj, w, fx);
         __syncthreads();
         // classical Gram-Schmidt, twice
         for (int pass = 0; pass < 2; ++pass) {
@@ -295,25 +296,12 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
         }
       }
       __syncthreads();
-      // X += M⁻¹ (V y); Z holds V y
+      // X += M⁻¹ V y = Z y: the preconditioned basis was kept, so the update needs no further
+      // preconditioner application (one band solve per cycle saved)
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double acc = 0.0;
-        for (int q = 0; q < k; ++q) acc += y[q] * (double)V[(int64_t)q * n + i];
-        Z[i] = (T)acc;
-      }
-      __syncthreads();
-      if (use_band) {
-        band_solve<T, T>(a.band, s, n0, n, Z, Z, xs, stp, ph);
-        for (int r = threadIdx.x; r < n; r += blockDim.x) X[r] += (double)Z[r];
-      } else {
-        for (int r = threadIdx.x; r < n; r += blockDim.x) {
-          const int nl = r / 6, kk = r % 6;
-          const T* Db = Dm + (n0 + nl) * 36 + kk;
-          double acc = 0.0;
-#pragma unroll
-          for (int j = 0; j < 6; ++j) acc += (double)Db[6 * j] * (double)Z[6 * nl + j];
-          X[r] += acc;
-        }
+        for (int q = 0; q < k; ++q) acc += y[q] * (double)Zb[(int64_t)q * n + i];
+        X[i] += acc;
       }
       __syncthreads();
       // true FP64 residual R = b - Ktan X

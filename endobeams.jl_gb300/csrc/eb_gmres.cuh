@@ -24,7 +24,7 @@ struct SolverArgs {
   double* X;             // n_dof work
   double* R64;           // n_dof work
   void* V;               // (m+1) n_dof Krylov basis (double or float)
-  void* Z;               // n_dof work (double or float)
+  void* Z;               // m n_dof preconditioned basis z_j = M⁻¹ v_j (double or float), m n_s per simulation
   int m, max_iter, max_ref;
   double tol, inner_tol;
   double* norms;         // 5 per sim: |ΔD_free|², |r_free|², |f_free|², |f_fixed|², iterations of the solve
