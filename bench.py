@@ -58,6 +58,12 @@ F_ELEM_FP64 = 1702.0 + 3085.0 + 2 * 5987.0
 # Elements in contact also write their 2.4 KB of tangents; those writes are not counted.
 B_CONTACT_ELEM = 480.0 + 88.0 + 13.0 + 648.0
 
+# DRAM bytes k_gmres moves per algorithmic byte (band, inverses, tangent): 158.2 GB read + written
+# against 151.9 GB algorithmic over the 24 k_gmres launches of 2 steps of 16 stents (ncu
+# dram__bytes_read.sum + dram__bytes_write.sum); the full workload's launches are too large to
+# capture, so the line scales its algorithmic bytes per launch by this ratio.
+KRYLOV_TRAFFIC_RATIO = 158.2 / 151.9
+
 METRIC = "HHT steps/s & Newton iters/step, batched+learned vs plain"
 MODEL = os.path.join(ROOT, "endobeams.jl_gb300", "models", "warm_start_stents.npz")
 # Newton tolerances of the stents.  The configurations ask for 1e-8.  The normalised residual of
@@ -87,11 +93,11 @@ def parse():
     ap.add_argument("--precision", default=None, choices=[None, "fp64", "mixed"])
     ap.add_argument("--warm-start", default=None, choices=[None, "off", "learned", "learned_x0"])
     ap.add_argument("--count", type=int, default=None, help="population size override (stents)")
-    ap.add_argument("--band-lu", default="fp32", choices=["fp32", "tensor"],
+    ap.add_argument("--band-lu", default="tensor", choices=["fp32", "tensor"],
                     help="band LU engine of the stents' preconditioner")
-    ap.add_argument("--refactor", default="threshold", choices=["threshold", "cost", "always"],
+    ap.add_argument("--refactor", default="cost", choices=["threshold", "cost", "always"],
                     help="stents: when a band LU is refactorised")
-    ap.add_argument("--refactor-cost", type=float, default=0.2,
+    ap.add_argument("--refactor-cost", type=float, default=0.03,
                     help="--refactor cost: GMRES iterations one LU is worth per DOF of half bandwidth")
     ap.add_argument("--mem-frac", type=float, default=0.75, help="device memory fraction per resident group")
     ap.add_argument("--cpu-sample", type=int, default=2, help="simulations in the CPU-baseline sample of the GPU arm")
@@ -123,16 +129,16 @@ def stent_tol_res(conf):
     return STENT_TOL_RES if le >= STENT_ELEM_1E8 else STENT_TOL_RES_SHORT
 
 
-SOLVER = dict(band_lu="fp32", refactor="threshold", refactor_cost=0.2)  # set from the command line
+SOLVER = dict(band_lu="tensor", refactor="cost", refactor_cost=0.03)  # set from the command line
 
 
 def stent_params(p, precision="mixed", warm="off"):
     p.tolerance_residual = STENT_TOL_RES
     p.tolerance_displacement = STENT_TOL_DISP
     p.krylov_restart = 32
-    # the stents' band LU costs ~0.1-1 s per factorisation on one SM with the FP32 engine: reuse it
-    # while GMRES needs <= 200 iterations (64 stents: 20.1 HHT steps/s never refactorising, 17.9 at
-    # 48, 14.5 at 16), or by the cost rule (iterations lost to ageing against the LU's cost)
+    # a stent's band LU costs ~0.1-1.5 s on one SM: it is reused, and refactorised by the cost rule
+    # when the GMRES iterations lost to its ageing reach its cost (64 stents, 20 steps: 15.2 HHT
+    # steps/s refactorising only past 200 iterations, 26.0 by the cost rule); 200 stays a cap
     p.refactor_its = 0 if SOLVER["refactor"] == "always" else 200
     p.refactor_policy = "cost" if SOLVER["refactor"] == "cost" else "threshold"
     p.refactor_cost = SOLVER["refactor_cost"]
@@ -583,10 +589,15 @@ def gpu_arm(args, rank, world):
         bytes_total = per_iter * iters_per_sim
         ach = bytes_total / (phase_ms["krylov"] * 1e-3) / 1e9
         hbm = peaks.get("hbm_gbs")
+        per_launch = bytes_total / max(launches["krylov"], 1)
         rooflines["krylov"] = {"kernel": "k_gmres (per-simulation restarted GMRES, band-LU preconditioned)",
                                "bound": "hbm", "achieved": ach, "peak": hbm,
                                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else None, "unit": "GB/s",
-                               "frac": (ach / hbm) if hbm else None, "traffic": None,
+                               "frac": (ach / hbm) if hbm else None,
+                               "traffic": KRYLOV_TRAFFIC_RATIO * per_launch,
+                               "traffic_note": "bytes per launch: the algorithmic bytes per launch x the DRAM/"
+                                               "algorithmic ratio ncu measured on 16 stents (1.04)",
+                               "algorithmic_bytes_per_launch": per_launch,
                                "algorithmic_bytes_per_iteration": per_iter / max(wl.count, 1),
                                "share_of_step": phase_ms["krylov"] / sum(phase_ms.values())}
     roof = rooflines.get("krylov") if dom in ("krylov", "precond") and "krylov" in rooflines else rooflines.get("beam")
