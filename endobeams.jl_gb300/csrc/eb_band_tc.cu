@@ -89,7 +89,6 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
   extern __shared__ __align__(1024) char smc[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smc);          // two MMA-completion barriers
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smc + 64);   // tensor-memory base address
-  int* sfail = reinterpret_cast<int*>(smc + 128);
   const int ldp = (int)tc_ldp(b);
   float* P = reinterpret_cast<float*>(smc + 1024);                        // panel, ldp x 32 column-major
   const size_t npad = tc_npad(b);
@@ -104,7 +103,6 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
-    *sfail = 0;
     fence_async_smem();
   }
   if (warp == 0) umma::tmem_alloc(tslot, kTmemCols);
@@ -129,17 +127,53 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         P[r + ldp * c] = (i - j <= b && j - i <= b) ? V.at(i, j) : 0.f;
       }
     __syncthreads();
-    // ---- 1. panel LU (column c = lane, rows strided by warps)
-    for (int t = 0; t < kb; ++t) {
-      const float ip = 1.f / P[t + ldp * t];
-      for (int r = t + 1 + threadIdx.x; r < hp; r += kTcThreads) P[r + ldp * t] *= ip;
-      __syncthreads();
-      if (lane > t && lane < kb) {
-        const float ut = P[t + ldp * lane];
-        for (int r = t + 1 + warp; r < hp; r += nw) P[r + ldp * lane] -= P[r + ldp * t] * ut;
-      }
-      __syncthreads();
+    // ---- 1. panel LU: warp w owns columns w and w + 16, its lanes run along the rows.  At
+    // column t every owner of a later column subtracts column t's multipliers times its row-t
+    // entry, and the owner of column t + 1 then scales that column by its pivot itself (same
+    // warp), so one block barrier per column publishes the next multipliers.  Each entry sees
+    // the same operations in the same order as a column-by-column elimination.
+    if (warp == 0 && kb > 0) {
+      const float ip = 1.f / P[0];
+      for (int r = 1 + lane; r < hp; r += 32) P[r] *= ip;
     }
+    for (int t = 0; t < kb; ++t) {
+      __syncthreads();  // column t's multipliers and row t are final
+      for (int c = warp; c < kb; c += nw) {
+        if (c <= t) continue;
+        const float ut = P[t + ldp * c];
+        for (int r = t + 1 + lane; r < hp; r += 32) P[r + ldp * c] -= P[r + ldp * t] * ut;
+        if (c == t + 1) {
+          __syncwarp();
+          const float ip = 1.f / P[c + ldp * c];
+          for (int r = c + 1 + lane; r < hp; r += 32) P[r + ldp * c] *= ip;
+        }
+      }
+    }
+    __syncthreads();
+    // inverses of L11 (unit lower, which = 0) and U11 (upper, which = 1), one column per lane,
+    // by column-oriented substitution: the updates of one step are independent, so the
+    // dependent chain is 32 steps long instead of 496 multiply-adds
+    auto inverses = [&](int which) {
+      float z[kPanel];
+#pragma unroll
+      for (int r = 0; r < kPanel; ++r) z[r] = (r == lane) ? 1.f : 0.f;
+      if (which == 0) {
+#pragma unroll
+        for (int t = 0; t < kPanel - 1; ++t)
+#pragma unroll
+          for (int r = t + 1; r < kPanel; ++r) z[r] -= (r < kb && t < kb ? P[r + ldp * t] : 0.f) * z[t];
+      } else {
+#pragma unroll
+        for (int t = kPanel - 1; t >= 0; --t) {
+          if (t < kb) z[t] = z[t] / P[t + ldp * t];
+#pragma unroll
+          for (int r = 0; r < t; ++r) z[r] -= (r < kb && t < kb ? P[r + ldp * t] : 0.f) * z[t];
+        }
+      }
+      float* dst = (which == 0 ? Li : Ui) + (int64_t)k0 * kPanel;
+#pragma unroll
+      for (int r = 0; r < kPanel; ++r) dst[lane * kPanel + r] = z[r];
+    };
     // ---- 2. U12 = L11⁻¹ A12 (q > 0 implies kb = 32), into the band and B, kU12 columns at a
     // time through the (idle) A operand buffer: each column is loaded and stored by one warp
     // (32 rows, one 128-byte line), solved by one thread from shared memory (stride 33: no bank
@@ -152,17 +186,19 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         S[lane + 33 * c] = (j - i <= b) ? V.at(i, j) : 0.f;
       }
       __syncthreads();
+      // the first chunk's solves occupy threads below kU12 (warps 0-5); the two top warps
+      // compute the panel inverses meanwhile
+      static_assert(kU12 <= kTcThreads - 64, "inverse warps must be idle in the U12 solve");
+      if (cs == 0 && warp >= nw - 2) inverses(warp - (nw - 2));
       for (int c = threadIdx.x; c < cn; c += kTcThreads) {
         float col[kPanel];
 #pragma unroll
         for (int r = 0; r < kPanel; ++r) col[r] = S[r + 33 * c];
+        // forward substitution column by column: the 31 - t updates of step t are independent
 #pragma unroll
-        for (int r = 1; r < kPanel; ++r) {
-          float acc = col[r];
+        for (int t = 0; t < kPanel - 1; ++t)
 #pragma unroll
-          for (int t = 0; t < r; ++t) acc -= P[r + ldp * t] * col[t];
-          col[r] = acc;
-        }
+          for (int r = t + 1; r < kPanel; ++r) col[r] -= P[r + ldp * t] * col[t];
 #pragma unroll
         for (int r = 0; r < kPanel; ++r) S[r + 33 * c] = col[r];
 #pragma unroll
@@ -186,32 +222,8 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
 #pragma unroll
       for (int g = 0; g < 4; ++g) store_triple(Bp, umma::kmajor_offset(c, 8 * g), z);
     }
-    // ---- 3. inverses of L11 (unit lower) and U11 (upper), as k_band_lu
-    if (warp == 0) {
-      float z[kPanel];
-#pragma unroll
-      for (int r = 0; r < kPanel; ++r) {
-        float acc = (r == lane) ? 1.f : 0.f;
-#pragma unroll
-        for (int t = 0; t < r; ++t) acc -= (r < kb && t < kb ? P[r + ldp * t] : 0.f) * z[t];
-        z[r] = acc;
-      }
-      float* L = Li + (int64_t)k0 * kPanel;
-#pragma unroll
-      for (int r = 0; r < kPanel; ++r) L[lane * kPanel + r] = z[r];
-    } else if (warp == 1) {
-      float z[kPanel];
-#pragma unroll
-      for (int r = kPanel - 1; r >= 0; --r) {
-        float acc = (r == lane) ? 1.f : 0.f;
-#pragma unroll
-        for (int t = r + 1; t < kPanel; ++t) acc -= (r < kb && t < kb ? P[r + ldp * t] : 0.f) * z[t];
-        z[r] = r < kb ? acc / P[r + ldp * r] : acc;
-      }
-      float* Uv = Ui + (int64_t)k0 * kPanel;
-#pragma unroll
-      for (int r = 0; r < kPanel; ++r) Uv[lane * kPanel + r] = z[r];
-    }
+    // ---- 3. without U12 work (last panel) the inverses run here, on warps 0 and 1
+    if (q <= 0 && warp < 2) inverses(warp);
     // ---- write back the panel (L11, U11, L21), warp per column as it was loaded
     for (int c = warp; c < kb; c += nw)
       for (int r = lane; r < hp; r += 32) {
@@ -267,12 +279,16 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
 #pragma unroll
         for (int c = 0; c < 32; ++c)
           old[c] = c < cmax ? (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) : 0.f;
-        if (!mbar_wait(&bar[buf], phase[buf])) *sfail = 1;
-        if (threadIdx.x == 0 && !*sfail) pending[buf] -= 1;
+        const bool done = mbar_wait(&bar[buf], phase[buf]);
+        if (threadIdx.x == 0 && done) pending[buf] -= 1;
         phase[buf] ^= 1u;
+        // this barrier also orders every thread's accumulator read of tile nc - 1 (same buffer
+        // as tile nc + 1) before the MMAs of tile nc + 1 are issued; all threads get the same
+        // verdict from it, so they leave the loop together
+        umma::fence_before_sync();
+        const int timed_out = __syncthreads_or(!done);
         umma::fence_after_sync();
-        __syncthreads();
-        if (*sfail) {
+        if (timed_out) {
           failed = true;
           break;
         }
@@ -284,9 +300,8 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
 #pragma unroll
         for (int c = 0; c < 32; ++c)
           if (c < cmax) (c < sp ? pL[(int64_t)(b - 1) * c] : pU[(int64_t)b * c]) = old[c] - acc[c];
-        umma::fence_before_sync();
-        __syncthreads();
-        umma::fence_after_sync();
+        // no barrier here: a warp goes on to load the next tile's old values (other columns)
+        // while the others still store this one
       }
     }
     __syncthreads();
