@@ -119,6 +119,23 @@ __device__ __forceinline__ void stage_drain(const Stage* st) {
     if (st->pend[k] >= 0) mbar_wait(&st->bar[k], (uint32_t)st->pend[k]);
 }
 
+// Σ_t col[t stride] y[t] over a full block (32 columns, none clipped by the band edge) as
+// a0 + a1, a0 over even t and a1 over odd t in increasing t: the operations of the general
+// loop below, unrolled so that the 32 shared loads of a row are in flight together.
+__device__ __forceinline__ float row_dot32(const float* col, int stride, const float* y) {
+  const float4* y4 = reinterpret_cast<const float4*>(y);
+  float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+  for (int t4 = 0; t4 < kPanel / 4; ++t4) {
+    const float4 w = y4[t4];
+    a0 = fmaf(col[(4 * t4) * stride], w.x, a0);
+    a1 = fmaf(col[(4 * t4 + 1) * stride], w.y, a1);
+    a0 = fmaf(col[(4 * t4 + 2) * stride], w.z, a0);
+    a1 = fmaf(col[(4 * t4 + 3) * stride], w.w, a1);
+  }
+  return a0 + a1;
+}
+
 // z = M⁻¹ v on the CTA owning simulation s: gather into band order, forward
 // substitution with unit L, backward substitution with U, scatter back.
 //
@@ -141,7 +158,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
   float* x = xs ? xs : B.work + 6 * n0;
   const float* Li = B.Linv + inv_base(n0, s);
   const float* Ui = B.Uinv + inv_base(n0, s);
-  __shared__ float yb[2][kPanel];  // y of the last two blocks
+  __shared__ __align__(16) float yb[2][kPanel];  // y of the last two blocks
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
     const int node = B.node_at[n0 + r / 6];           // global id of the node at position r/6
     x[r] = (float)v[6 * (node - n0) + r % 6];
@@ -240,7 +257,9 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
           if (fwd) {  // L(i, pk0 + t), d = i - pk0 - t in [1, b]
             const int tlo = max(0, i - pk0 - b);
             int t = tlo;
-            if (Pc) {
+            if (Pc && tlo == 0 && pkb == kPanel) {
+              a0 = row_dot32(Pc + (i - pk0 - 1), b - 1, yp);
+            } else if (Pc) {
               const float* col = Pc + (i - pk0 - 1);
               for (; t + 1 < pkb; t += 2) {
                 a0 = fmaf(col[t * (b - 1)], yp[t], a0);
@@ -257,7 +276,9 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
           } else {  // U(i, pk0 + t), d = pk0 + t - i in [1, b]
             const int thi = min(pkb, i + b - pk0 + 1);
             int t = 0;
-            if (Pc) {
+            if (Pc && thi == kPanel) {
+              a0 = row_dot32(Pc + (b - pk0 + i), b, yp);
+            } else if (Pc) {
               const float* col = Pc + (b - pk0 + i);
               for (; t + 1 < thi; t += 2) {
                 a0 = fmaf(col[t * b], yp[t], a0);
@@ -308,7 +329,9 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             const int tlo = max(0, i - pk0 - b);
             float a0 = 0.f, a1 = 0.f;
             int t = tlo;
-            if (Pc) {
+            if (Pc && tlo == 0 && pkb == kPanel) {
+              a0 = row_dot32(Pc + (i - pk0 - 1), b - 1, yp);
+            } else if (Pc) {
               const float* col = Pc + (i - pk0 - 1);
               for (; t + 1 < pkb; t += 2) {
                 a0 = fmaf(col[t * (b - 1)], yp[t], a0);
@@ -330,7 +353,9 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
             const int thi = min(pkb, i + b - pk0 + 1);
             float a0 = 0.f, a1 = 0.f;
             int t = 0;
-            if (Pc) {
+            if (Pc && thi == kPanel) {
+              a0 = row_dot32(Pc + (b - pk0 + i), b, yp);
+            } else if (Pc) {
               const float* col = Pc + (b - pk0 + i);
               for (; t + 1 < thi; t += 2) {
                 a0 = fmaf(col[t * b], yp[t], a0);
