@@ -119,19 +119,34 @@ __device__ __forceinline__ void stage_drain(const Stage* st) {
     if (st->pend[k] >= 0) mbar_wait(&st->bar[k], (uint32_t)st->pend[k]);
 }
 
+// Explicit shared-memory loads.  The staging buffers are reached through generic pointers,
+// and a generic load that lands in shared memory is scoreboarded like a global one.
+__device__ __forceinline__ float lds_f32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ float4 lds_f32x4(uint32_t a) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a)
+               : "memory");
+  return v;
+}
+
 // Σ_t col[t stride] y[t] over a full block (32 columns, none clipped by the band edge) as
 // a0 + a1, a0 over even t and a1 over odd t in increasing t: the operations of the general
-// loop below, unrolled so that the 32 shared loads of a row are in flight together.
+// loop below, unrolled so that the 32 shared loads of a row are in flight together.  `col`
+// and `y` (16-byte aligned) are in shared memory.
 __device__ __forceinline__ float row_dot32(const float* col, int stride, const float* y) {
-  const float4* y4 = reinterpret_cast<const float4*>(y);
+  const uint32_t c = smem_u32(col), ya = smem_u32(y), sb = 4u * (uint32_t)stride;
   float a0 = 0.f, a1 = 0.f;
 #pragma unroll
   for (int t4 = 0; t4 < kPanel / 4; ++t4) {
-    const float4 w = y4[t4];
-    a0 = fmaf(col[(4 * t4) * stride], w.x, a0);
-    a1 = fmaf(col[(4 * t4 + 1) * stride], w.y, a1);
-    a0 = fmaf(col[(4 * t4 + 2) * stride], w.z, a0);
-    a1 = fmaf(col[(4 * t4 + 3) * stride], w.w, a1);
+    const float4 w = lds_f32x4(ya + 16u * t4);
+    a0 = fmaf(lds_f32(c + (4 * t4) * sb), w.x, a0);
+    a1 = fmaf(lds_f32(c + (4 * t4 + 1) * sb), w.y, a1);
+    a0 = fmaf(lds_f32(c + (4 * t4 + 2) * sb), w.z, a0);
+    a1 = fmaf(lds_f32(c + (4 * t4 + 3) * sb), w.w, a1);
   }
   return a0 + a1;
 }
@@ -148,11 +163,13 @@ __device__ __forceinline__ float row_dot32(const float* col, int stride, const f
 // backward sweep is the mirror image.  `xs` (may be null) is shared-memory
 // room for the n permuted entries; without it the rows the sweeps touch live
 // in a shared ring.  With `st` non-null, band columns and inverses are
-// streamed into shared memory by bulk async copies one step ahead; `ph`
-// (4 entries) holds the barriers' next phase bits and is advanced here.
+// streamed into shared memory by bulk async copies one step ahead; bit k of
+// `ph` is barrier k's next phase and is advanced here.  Everything the sweeps
+// keep per thread (stage pointers, phase bits) is selected without indexing,
+// so it stays in registers: no local-memory load sits on the block chain.
 template <typename TV, typename TZ>
-__device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV* __restrict__ v, TZ* __restrict__ z,
-                           float* xs, const Stage* st, uint32_t* ph) {
+__device__ __forceinline__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV* __restrict__ v,
+                                           TZ* __restrict__ z, float* xs, const Stage* st, uint32_t& ph) {
   const BandView V = band_view(B, s, n);
   const int b = V.b;
   float* x = xs ? xs : B.work + 6 * n0;
@@ -179,6 +196,10 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     for (int r = threadIdx.x; r < min(n, W); r += blockDim.x) xw[r & wm] = x[r];
     __syncthreads();
   }
+  const Stage S = st ? *st : Stage{};
+  auto sbuf = [&](int k) { return (k & 1) ? S.buf[1] : S.buf[0]; };
+  auto sinv = [&](int k) { return (k & 1) ? S.inv[1] : S.inv[0]; };
+  auto phb = [&](int k) { return (ph >> k) & 1u; };
   // bulk copies: band columns of block jb (L or U part) into buffer sb, or its inverse into buffer sb
   auto issue_cols = [&](int jb, int sb, bool lower) {
     const int k0 = jb * kPanel;
@@ -187,25 +208,25 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     const float* src = lower ? V.L + (int64_t)b * k0 : V.U + (int64_t)(b + 1) * k0;
     const uint32_t bytes = (uint32_t)(((int64_t)kb * colw * 4 + 15) & ~(int64_t)15);
     fence_async_smem();
-    mbar_expect_tx(&st->bar[sb], bytes);
-    bulk_g2s(st->buf[sb], src, bytes, &st->bar[sb]);
-    st->pend[sb] = (int)ph[sb];
+    mbar_expect_tx(S.bar + sb, bytes);
+    bulk_g2s(sbuf(sb), src, bytes, S.bar + sb);
+    S.pend[sb] = (int)phb(sb);
   };
   auto issue_inv = [&](int jb, int sb, bool lower, uint32_t extra) {
     const float* isrc = (lower ? Li : Ui) + (int64_t)jb * kPanel * kPanel;
     fence_async_smem();
-    mbar_expect_tx(&st->bar[2 + sb], 4096u + extra);
-    bulk_g2s(st->inv[sb], isrc, 4096u, &st->bar[2 + sb]);
-    st->pend[2 + sb] = (int)ph[2 + sb];
+    mbar_expect_tx(S.bar + 2 + sb, 4096u + extra);
+    bulk_g2s(sinv(sb), isrc, 4096u, S.bar + 2 + sb);
+    S.pend[2 + sb] = (int)phb(2 + sb);
   };
   auto await = [&](int k) {  // k: barrier index 0..3
-    if (!*st->fail) {
-      if (!mbar_wait(&st->bar[k], ph[k]) && !mbar_wait(&st->bar[k], ph[k])) *st->fail = 1;
-      else if (threadIdx.x == 0) st->pend[k] = -1;
+    if (!*S.fail) {
+      if (!mbar_wait(S.bar + k, phb(k)) && !mbar_wait(S.bar + k, phb(k))) *S.fail = 1;
+      else if (threadIdx.x == 0) S.pend[k] = -1;
     }
-    ph[k] ^= 1u;
+    ph ^= 1u << k;
   };
-  const bool staged = st && !*st->fail;  // uniform: read after the barrier above
+  const bool staged = st && !*S.fail;  // uniform: read after the barrier above
   // the copies are issued by the CTA's last thread, off warp 0's chain
   const bool issuer = threadIdx.x == blockDim.x - 1;
 
@@ -218,8 +239,8 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
     }
     // block visited at step q (forward: q, backward: nblk - 1 - q)
     auto blk = [&](int q) { return fwd ? q : nblk - 1 - q; };
-    if (staged && issuer && !*st->fail) {
-      issue_inv(blk(0), 0, fwd, fwd ? st->extra : 0u);
+    if (staged && issuer && !*S.fail) {
+      issue_inv(blk(0), 0, fwd, fwd ? S.extra : 0u);
       if (nblk > 1) {
         issue_inv(blk(1), 1, fwd, 0u);
         issue_cols(blk(0), 0, fwd);
@@ -240,10 +261,10 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       if (staged) {
         if (q > 0) await((q - 1) & 1);
         if (warp == 0) await(2 + (q & 1));
-        else ph[2 + (q & 1)] ^= 1u;  // the other threads only follow the inverse barriers' phases
-        if (!*st->fail) {
-          if (q > 0) Pc = st->buf[(q - 1) & 1];
-          Inv = st->inv[q & 1];
+        else ph ^= 1u << (2 + (q & 1));  // the other threads only follow the inverse barriers' phases
+        if (!*S.fail) {
+          if (q > 0) Pc = sbuf(q - 1);
+          Inv = sinv(q);
         }
       }
       const float* yp = yb[(q + 1) & 1];  // y of block pj (written at step q - 1)
@@ -375,7 +396,7 @@ __device__ void band_solve(const BandDev& B, int s, int64_t n0, int n, const TV*
       }
       __syncthreads();
       // buffers freed at this step: band columns of block pj, inverse of block jb
-      if (staged && issuer && !*st->fail) {
+      if (staged && issuer && !*S.fail) {
         if (q + 1 <= nblk - 2) issue_cols(blk(q + 1), (q + 1) & 1, fwd);
         if (q + 2 <= nblk - 1) issue_inv(blk(q + 2), q & 1, fwd, 0u);
       }

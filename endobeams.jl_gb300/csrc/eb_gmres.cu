@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
   __shared__ int stage_pend[4];
   Stage stage;
   const Stage* stp = nullptr;
-  uint32_t ph[4] = {0u, 0u, 0u, 0u};
+  uint32_t ph = 0u;  // bit k: next phase of staging barrier k
   if (use_band && a.stage_floats > 0) {
     char* base = reinterpret_cast<char*>(xs ? xs + a.max_n : reinterpret_cast<float*>(red + 8 * 32));
     base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 127) & ~uintptr_t(127));
@@ -244,7 +244,9 @@ __global__ void __launch_bounds__(512) k_gmres(SolverArgs a) {
             if (threadIdx.x == 0)
               for (int q = 0; q < nq; ++q) H[(m + 1) * j + i0 + q] = (pass == 0 ? 0.0 : H[(m + 1) * j + i0 + q]) + hp[q];
             // stash this chunk's coefficients in y (free until the back-substitution)
-            if (threadIdx.x < nq) y[i0 + threadIdx.x] = hp[threadIdx.x];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+              if (threadIdx.x == q && q < nq) y[i0 + q] = hp[q];
             __syncthreads();
           }
           for (int i = threadIdx.x; i < n; i += blockDim.x) {
