@@ -13,8 +13,10 @@ Workloads (synthetic, seeded; no dataset):
             E = 50 GPa, each released stress free into its own cylinder SDF
             (radius U[0.85,0.95] of the stent's, 0.1 mm grid sized to the stent);
             mu = 0.1, dt = 1e-5 s, FP32 GMRES inside FP64 refinement.  The
-            population runs as resident groups sized to the device memory;
-            the learned warm start (committed model) gives the initial guess
+            population runs as resident groups sized to the device memory,
+            each group as concurrent lanes (--lanes, default 4: one engine,
+            host thread and CUDA stream each, so one lane's kernels fill the
+            SMs another lane's Newton tail leaves idle); the learned warm start (committed model) gives the initial guess
             of each predictor solve.  The line also carries the same groups
             and step window with the plain HHT predictor, and the plain
             single-stent path (48 wires, R = 4 mm, 45 deg, 200 elements per
@@ -100,6 +102,8 @@ def parse():
     ap.add_argument("--refactor-cost", type=float, default=0.08,
                     help="--refactor cost: GMRES iterations one LU is worth per DOF of half bandwidth")
     ap.add_argument("--mem-frac", type=float, default=0.75, help="device memory fraction per resident group")
+    ap.add_argument("--lanes", type=int, default=4,
+                    help="concurrent lanes per resident group (one engine, host thread and stream each)")
     ap.add_argument("--cpu-sample", type=int, default=2, help="simulations in the CPU-baseline sample of the GPU arm")
     ap.add_argument("--cpu-steps", type=int, default=3, help="steps per simulation in that CPU-baseline sample")
     ap.add_argument("--ref-sample", type=int, default=48,
@@ -396,62 +400,121 @@ class Driver:
         return k
 
 
+def _lib_phases():
+    from endobeams_gb300 import _lib
+    return list(_lib.PHASES)
+
+
+def _in_lanes(fn, items):
+    """fn(item) for every item, each on its own host thread (the library releases the
+    interpreter during its calls, so the lanes' steps overlap on the GPU)."""
+    import threading
+    from endobeams_gb300 import _lib
+    device = _lib.current_device()
+    errors = []
+
+    def run(it):
+        try:
+            _lib.set_device(device)
+            fn(it)
+        except BaseException as e:
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(it,)) for it in items]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    if errors:
+        raise errors[0]
+
+
 def run_group(eb, wl, idx, args, world, e2e=True, warm=None):
     """Creates one resident group, warms up W steps, times K steps; returns a dict of totals.
 
-    Every timed step goes through the public API with host buffers: the step's loads are
-    uploaded from host memory (eb_set_loads_all) and all displacements are read back
-    (eb_get_displacements).  The same K steps give both figures: the device time between
-    CUDA events on the handle's stream (`ms`, the whole-job HHT steps/s) and the host wall
-    clock around them (`e2e`)."""
+    The group runs as `--lanes` concurrent lanes (api.lane_split: round-robin in decreasing
+    size), one engine each, stepped by its own host thread on its own stream.  Every timed
+    step goes through the public API with host buffers: the step's loads are uploaded from
+    host memory (eb_set_loads_all) and all displacements are read back
+    (eb_get_displacements).  The same K steps give both figures: the device span between
+    CUDA events (the earliest lane's start to the latest lane's stop: `ms`, the whole-job
+    HHT steps/s) and the host wall clock around them (`e2e`)."""
     built = [wl.build(i) for i in idx]
-    confs = [b[0] for b in built]
-    inters = [b[2] for b in built]
     params = built[0][1]
     if warm is not None:
         params.warm_start = warm
     params.timing = True
-    eng = eb.GpuSimulations(confs, params, inters)
-    if wl.kind == "stents":
-        eng.set_tolerances(residual=[wl.tol_res[i] for i in idx])
-    if params.warm_start in ("learned", "learned_x0"):
-        from endobeams_gb300 import warm_start as W
-        eng.set_warm_start(W.WarmStartModel.load(MODEL))
-    mem, band_sims = eng.memory()
-    drv = Driver(eng, params, [len(c.beams) for c in confs])
-    total_nodes = sum(len(c.nodes) for c in confs)
-    ubuf = np.zeros((total_nodes, 3))
+    parts = eb.api.lane_split([len(b[0].beams) for b in built], args.lanes)
+    lanes = []
+    for part in parts:
+        confs = [built[j][0] for j in part]
+        inters = [built[j][2] for j in part]
+        eng = eb.GpuSimulations(confs, params, inters)
+        if wl.kind == "stents":
+            eng.set_tolerances(residual=[wl.tol_res[idx[j]] for j in part])
+        if params.warm_start in ("learned", "learned_x0"):
+            from endobeams_gb300 import warm_start as W
+            eng.set_warm_start(W.WarmStartModel.load(MODEL))
+        nodes = sum(len(c.nodes) for c in confs)
+        lanes.append({"eng": eng, "drv": Driver(eng, params, [len(c.beams) for c in confs]),
+                      "ubuf": np.zeros((nodes, 3)), "nodes": nodes, "elements": sum(len(c.beams) for c in confs),
+                      "loaded": sum(len(c.loads.concentrated_force.loaded_dofs) for c in confs if c.loads is not None)})
     use_e2e = e2e and not args.no_e2e
-    for _ in range(args.warmup):
-        drv.step(e2e=use_e2e, ubuf=ubuf)
-    launch_shapes = eng.autotune()
-    eng.phase_times(reset=True)
-    drv.reset()
+
+    def steps(n):
+        def go(ln):
+            for _ in range(n):
+                ln["drv"].step(e2e=use_e2e, ubuf=ln["ubuf"])
+        _in_lanes(go, lanes)
+
+    steps(args.warmup)
+    launch_shapes = [ln["eng"].autotune() for ln in lanes][0]
+    for ln in lanes:
+        ln["eng"].phase_times(reset=True)
+        ln["drv"].reset()
     barrier(world)
-    eng.timer_start()
+    for ln in lanes:
+        ln["eng"].timer_start()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        drv.step(e2e=use_e2e, ubuf=ubuf)
-    ms = allreduce_max(eng.timer_stop(), world)
-    wall = allreduce_max(time.perf_counter() - t0, world)
-    phase_ms, launches = eng.phase_times(reset=True)
-    out = {"sim_steps": drv.ok_steps, "ms": ms, "newton": drv.newton, "krylov": drv.krylov,
-           "pred_krylov": drv.pred_krylov,
-           "ws_used": drv.ws_used, "ws_steps": drv.ws_steps, "phase_ms": phase_ms, "launches": launches,
-           "elem_evals": drv.elem_evals, "nodes": total_nodes, "elements": sum(len(c.beams) for c in confs),
+    steps(args.steps)
+    wall = time.perf_counter() - t0
+    for ln in lanes:
+        ln["eng"].timer_stop()
+    span = max(a["eng"].timer_between(b["eng"]) for a in lanes for b in lanes)
+    ms = allreduce_max(span, world)
+    wall = allreduce_max(wall, world)
+    # per phase: the time during which any lane ran it (union of the lanes' intervals on one
+    # time axis); the summed lane times below exceed the span when the lanes overlap
+    ref = lanes[0]["eng"]
+    phase_union = {k: eb.api.union_ms([ln["eng"].phase_intervals(k, ref) for ln in lanes]) for k in _lib_phases()}
+    phase_ms, launches = None, None
+    for ln in lanes:  # each lane's phase intervals on its own stream (the lanes overlap)
+        pm, la = ln["eng"].phase_times(reset=True)
+        phase_ms = dict(pm) if phase_ms is None else {k: phase_ms[k] + pm[k] for k in pm}
+        launches = dict(la) if launches is None else {k: launches[k] + la[k] for k in la}
+    D = [ln["drv"] for ln in lanes]
+    tot = lambda f: sum(getattr(d, f) for d in D)
+    mem = sum(ln["eng"].memory()[0] for ln in lanes)
+    band_sims = sum(ln["eng"].memory()[1] for ln in lanes)
+    out = {"sim_steps": tot("ok_steps"), "ms": ms, "newton": tot("newton"), "krylov": tot("krylov"),
+           "pred_krylov": tot("pred_krylov"), "ws_used": tot("ws_used"), "ws_steps": tot("ws_steps"),
+           "phase_ms": phase_ms, "launches": launches, "elem_evals": tot("elem_evals"),
+           "nodes": sum(ln["nodes"] for ln in lanes), "elements": sum(ln["elements"] for ln in lanes),
            "sims": len(idx), "device_bytes": mem, "band_sims": band_sims, "e2e": None,
-           "launch_shapes": launch_shapes}
+           "launch_shapes": launch_shapes, "lanes": len(lanes), "phase_union_ms": phase_union}
     if use_e2e:
-        n_loaded = sum(len(c.loads.concentrated_force.loaded_dofs) for c in confs if c.loads is not None)
-        S = drv.S
-        bi = drv.batch_iters / max(args.steps, 1)
-        # loads, per-sim step constants (cK, cC, cM, dt), active masks (step + each iteration), commit mask
-        h2d = 8 * n_loaded + 32 * S + 4 * S + 4 * S * bi + 4 * S
-        # displacements, per-iteration Newton norms, per-step solver statistics
-        d2h = 24 * total_nodes + 40 * S * bi + 20 * S
-        out["e2e"] = {"sim_steps": drv.ok_steps, "wall_s": wall, "h2d": h2d, "d2h": d2h, "device_ms": ms,
-                      "newton": drv.newton, "krylov": drv.krylov}
-    eng.close()
+        h2d = d2h = 0
+        for ln in lanes:
+            S = ln["drv"].S
+            bi = ln["drv"].batch_iters / max(args.steps, 1)
+            # loads, per-sim step constants (cK, cC, cM, dt), active masks (step + each iteration), commit mask
+            h2d += 8 * ln["loaded"] + 32 * S + 4 * S + 4 * S * bi + 4 * S
+            # displacements, per-iteration Newton norms, per-step solver statistics
+            d2h += 24 * ln["nodes"] + 40 * S * bi + 20 * S
+        out["e2e"] = {"sim_steps": out["sim_steps"], "wall_s": wall, "h2d": h2d, "d2h": d2h, "device_ms": ms,
+                      "newton": out["newton"], "krylov": out["krylov"]}
+    for ln in lanes:
+        ln["eng"].close()
     return out
 
 
@@ -534,6 +597,7 @@ def gpu_arm(args, rank, world):
             tot = r
             tot["e2e"] = dict(r["e2e"]) if r["e2e"] else None
             tot["phase_ms"] = dict(r["phase_ms"])
+            tot["phase_union_ms"] = dict(r["phase_union_ms"])
             tot["launches"] = dict(r["launches"])
             tot["device_bytes_max"] = r["device_bytes"]
         else:
@@ -543,6 +607,7 @@ def gpu_arm(args, rank, world):
             tot["device_bytes_max"] = max(tot["device_bytes_max"], r["device_bytes"])
             for k in tot["phase_ms"]:
                 tot["phase_ms"][k] += r["phase_ms"][k]
+                tot["phase_union_ms"][k] += r["phase_union_ms"][k]
                 tot["launches"][k] += r["launches"][k]
             if tot["e2e"] and r["e2e"]:
                 for k in ("sim_steps", "wall_s", "h2d", "d2h", "device_ms", "newton", "krylov"):
@@ -560,13 +625,17 @@ def gpu_arm(args, rank, world):
                        "read back every step, host wall clock"}
     phase_ms, launches = tot["phase_ms"], tot["launches"]
     dom = max(phase_ms, key=lambda k: phase_ms[k])
+    # The phase times are each lane's intervals on its own stream; the lanes overlap, so the
+    # rooflines take each phase's union over the lanes (the time during which any lane ran it):
+    # the work of all lanes over that time is the rate the GPU sustained on the phase.
+    dev_ms = {k: max(v, 1e-9) for k, v in tot["phase_union_ms"].items()}
     # ---- rooflines: the element kernel (FP64 pipe) and the Krylov kernel (HBM)
     peak_fp64 = eb.fp64_peak_tflops()
     rooflines = {}
     if launches["beam"] and tot["elem_evals"]:
         # FP64 flops of every element evaluation of the timed corrector iterations over the phase's device time
         avg_beam_ms = phase_ms["beam"] / launches["beam"]
-        ach = F_ELEM_FP64 * tot["elem_evals"] / (phase_ms["beam"] * 1e-3) / 1e12
+        ach = F_ELEM_FP64 * tot["elem_evals"] / (dev_ms["beam"] * 1e-3) / 1e12
         rooflines["beam"] = {"kernel": "k_beam (corotational element, FP64)", "bound": "fp64", "achieved": ach,
                              "peak": peak_fp64, "peak_source": "measured (eb_fp64_peak FMA probe on this GPU)",
                              "unit": "TFLOP/s", "frac": ach / peak_fp64, "traffic": None,
@@ -574,7 +643,7 @@ def gpu_arm(args, rank, world):
     peaks = _measured_peaks()
     if launches["contact"] and tot["elem_evals"] and wl.kind == "stents":
         # every stent element is a contact element: one contact evaluation per element evaluation
-        ach = B_CONTACT_ELEM * tot["elem_evals"] / (phase_ms["contact"] * 1e-3) / 1e9
+        ach = B_CONTACT_ELEM * tot["elem_evals"] / (dev_ms["contact"] * 1e-3) / 1e9
         hbm = peaks.get("hbm_gbs")
         rooflines["contact"] = {"kernel": "k_contact (beam-to-SDF contact element, FP64)", "bound": "hbm",
                                 "achieved": ach, "peak": hbm,
@@ -588,7 +657,7 @@ def gpu_arm(args, rank, world):
         per_iter = gmres_bytes_per_iter(wl, range(wl.count))
         iters_per_sim = tot["krylov"] / max(tot["sims"], 1)  # summed over the timed steps
         bytes_total = per_iter * iters_per_sim
-        ach = bytes_total / (phase_ms["krylov"] * 1e-3) / 1e9
+        ach = bytes_total / (dev_ms["krylov"] * 1e-3) / 1e9
         hbm = peaks.get("hbm_gbs")
         per_launch = bytes_total / max(launches["krylov"], 1)
         rooflines["krylov"] = {"kernel": "k_gmres (per-simulation restarted GMRES, band-LU preconditioned)",
@@ -599,6 +668,11 @@ def gpu_arm(args, rank, world):
                                "traffic_note": "bytes per launch: the algorithmic bytes per launch x the DRAM/"
                                                "algorithmic ratio ncu measured on 16 stents (1.04)",
                                "algorithmic_bytes_per_launch": per_launch,
+                               "avg_launch_ms": phase_ms["krylov"] / max(launches["krylov"], 1),
+                               "time_basis": "union over the lanes of their Krylov intervals (lanes overlap: "
+                                             "each lane's launches run beside the others'); avg_launch_ms is one "
+                                             "lane's launch on its own stream",
+                               "phase_union_ms": dev_ms["krylov"],
                                "algorithmic_bytes_per_iteration": per_iter / max(wl.count, 1),
                                "share_of_step": phase_ms["krylov"] / sum(phase_ms.values())}
     roof = rooflines.get("krylov") if dom in ("krylov", "precond") and "krylov" in rooflines else rooflines.get("beam")
@@ -610,11 +684,14 @@ def gpu_arm(args, rank, world):
         "config": dict(wl.describe(tot["nodes"], tot["elements"], len(groups)),
                        l2="state, band and staging arrays exceed L2 (129 MB) each step", device=gname,
                        device_bytes_per_group_max=int(tot["device_bytes_max"]), band_preconditioned_sims=tot["band_sims"],
-                       launch_shapes_first_group=tot["launch_shapes"]),
+                       launch_shapes_first_group=tot["launch_shapes"], lanes_per_group=tot["lanes"]),
         "newton_iters_per_step": tot["newton"] / max(tot["sim_steps"], 1),
         "krylov_iters_per_newton": tot["krylov"] / max(tot["newton"], 1),
         "predictor_krylov_iters_per_step": tot["pred_krylov"] / max(tot["sim_steps"], 1),
-        "phase_ms": {k: round(v, 3) for k, v in phase_ms.items()}, "dominant_phase": dom,
+        "phase_ms": {k: round(v, 3) for k, v in phase_ms.items()},
+        "phase_ms_basis": "summed over the lanes' own streams (the lanes overlap, so the sum exceeds the span)",
+        "phase_union_ms": {k: round(v, 3) for k, v in tot["phase_union_ms"].items()},
+        "dominant_phase": dom,
         "gpu_launches": int(sum(launches.values())),
         "roofline": roof, "rooflines": rooflines, "e2e": e2e, "clocks": clk,
     }

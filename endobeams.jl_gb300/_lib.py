@@ -101,8 +101,11 @@ SIGNATURES = {
     "eb_ws_capture": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),
     "eb_ws_samples": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P_f, P_f, P_i64]),
     "eb_set_device": (C.c_int, [C.c_int32]),
+    "eb_get_device": (C.c_int, [P_i32]),
     "eb_timer_start": (C.c_int, [C.c_void_p]),
     "eb_timer_stop": (C.c_int, [C.c_void_p, P_d]),
+    "eb_timer_between": (C.c_int, [C.c_void_p, C.c_void_p, P_d]),
+    "eb_get_phase_intervals": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, P_d, P_d, C.c_int64, P_i64]),
     "eb_get_phase_times": (C.c_int, [C.c_void_p, P_d, P_i64, C.c_int32]),
     "eb_set_loads_all": (C.c_int, [C.c_void_p, P_d]),
     "eb_get_displacements": (C.c_int, [C.c_void_p, P_d]),
@@ -176,6 +179,18 @@ def device_info():
     name = C.create_string_buffer(256)
     rc = L.eb_device_info(C.byref(n), name, 256)
     return (n.value, name.value.decode()) if rc == EB_OK else (0, "")
+
+
+def current_device() -> int:
+    """The calling thread's current CUDA device."""
+    d = C.c_int32(0)
+    check(load().eb_get_device(C.byref(d)), "eb_get_device")
+    return int(d.value)
+
+
+def set_device(device: int) -> None:
+    """Makes ``device`` current for the calling thread (handles it creates or steps)."""
+    check(load().eb_set_device(int(device)), "eb_set_device")
 
 
 def device_memory():

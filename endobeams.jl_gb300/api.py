@@ -581,11 +581,30 @@ class GpuSimulations:
         check(self.L.eb_timer_stop(self.h, C.byref(ms)), "eb_timer_stop")
         return ms.value
 
+    def timer_between(self, last: "GpuSimulations") -> float:
+        """Device ms from this engine's timer_start to ``last``'s timer_stop (engines stepped
+        concurrently on their own streams)."""
+        ms = C.c_double(0.0)
+        check(self.L.eb_timer_between(self.h, last.h, C.byref(ms)), "eb_timer_between")
+        return ms.value
+
     def phase_times(self, reset: bool = False):
         ms = np.zeros(8)
         n = np.zeros(8, np.int64)
         check(self.L.eb_get_phase_times(self.h, ptr(ms), ptr(n, C.c_int64), 1 if reset else 0), "eb_get_phase_times")
         return dict(zip(_lib.PHASES, ms)), dict(zip(_lib.PHASES, n))
+
+    def phase_intervals(self, phase: str, ref: Optional["GpuSimulations"] = None) -> np.ndarray:
+        """(n, 2) start/end ms of every `phase` interval since this engine's timer_start, on the
+        time axis of ``ref``'s timer_start (default: this engine's)."""
+        k = _lib.PHASES.index(phase)
+        ref = ref or self
+        cnt = C.c_int64(0)
+        check(self.L.eb_get_phase_intervals(self.h, ref.h, k, None, None, 0, C.byref(cnt)), "eb_get_phase_intervals")
+        a, b = np.zeros(cnt.value), np.zeros(cnt.value)
+        check(self.L.eb_get_phase_intervals(self.h, ref.h, k, ptr(a), ptr(b), cnt.value, C.byref(cnt)),
+              "eb_get_phase_intervals")
+        return np.stack([a, b], axis=1)
 
     def autotune(self) -> dict:
         """Picks the fastest block sizes of the element, contact and assembly kernels on the current
@@ -710,11 +729,86 @@ def output_dirs(output_dir: str, n: int) -> List[str]:
     return [os.path.join(output_dir, f"sim_{s:05d}") for s in range(n)]
 
 
+def union_ms(intervals: Sequence[np.ndarray]) -> float:
+    """Length of the union of (start, end) intervals (ms), e.g. one phase over concurrent lanes."""
+    iv = np.concatenate([np.asarray(x, float).reshape(-1, 2) for x in intervals]) if len(intervals) else np.zeros((0, 2))
+    if not len(iv):
+        return 0.0
+    iv = iv[np.argsort(iv[:, 0])]
+    total, s0, e0 = 0.0, iv[0, 0], iv[0, 1]
+    for s1, e1 in iv[1:]:
+        if s1 > e0:
+            total += e0 - s0
+            s0, e0 = s1, e1
+        else:
+            e0 = max(e0, e1)
+    return float(total + e0 - s0)
+
+
+def lane_split(sizes: Sequence[int], lanes: int) -> List[List[int]]:
+    """Simulation indices of each lane: dealt round-robin in decreasing size, so that every
+    lane holds a similar mix of costly and cheap simulations."""
+    order = sorted(range(len(sizes)), key=lambda s: (-int(sizes[s]), s))
+    lanes = max(1, min(int(lanes), len(order)))
+    return [order[l::lanes] for l in range(lanes)]
+
+
+def _run_lanes(confs, params, inters, max_steps, on_step, points_per_beam, dirs, lanes) -> RunResult:
+    """run_simulations over concurrent lanes: one engine per lane, each stepped by its own
+    host thread on its own stream (the library releases the interpreter during its calls)."""
+    import threading
+    S = len(confs)
+    inters = list(inters) if inters is not None else [None] * S
+    parts = lane_split([len(c.beams) for c in confs], lanes)
+    if params.output_dir and dirs is None:
+        dirs = output_dirs(params.output_dir, S)
+    device = _lib.current_device()
+    results: List[Optional[RunResult]] = [None] * len(parts)
+    errors: List[BaseException] = []
+
+    def lane(l, idx):
+        try:
+            _lib.set_device(device)
+            results[l] = run_simulations([confs[i] for i in idx], params, [inters[i] for i in idx], max_steps,
+                                         on_step=on_step, points_per_beam=points_per_beam,
+                                         dirs=[dirs[i] for i in idx] if dirs is not None else None)
+        except BaseException as e:  # re-raised on the calling thread
+            errors.append(e)
+
+    t0 = time.perf_counter()
+    threads = [threading.Thread(target=lane, args=(l, idx)) for l, idx in enumerate(parts)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    if errors:
+        raise errors[0]
+    merged = RunResult(steps=[0] * S, ks=[[] for _ in range(S)], t=[0.0] * S, wall_s=time.perf_counter() - t0,
+                       newton_iterations=[0] * S, krylov_iterations=[0] * S, aborted=[False] * S)
+    for idx, r in zip(parts, results):
+        for j, i in enumerate(idx):
+            merged.steps[i], merged.ks[i], merged.t[i] = r.steps[j], r.ks[j], r.t[j]
+            merged.newton_iterations[i], merged.krylov_iterations[i] = r.newton_iterations[j], r.krylov_iterations[j]
+            merged.aborted[i] = r.aborted[j]
+    return merged
+
+
 def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Optional[int] = None,
-                    engine: Optional[GpuSimulations] = None, on_step=None, points_per_beam: int = 10) -> RunResult:
+                    engine: Optional[GpuSimulations] = None, on_step=None, points_per_beam: int = 10,
+                    lanes: int = 1, dirs: Optional[List[str]] = None) -> RunResult:
     """The time loop of run_simulation! (run_simulation.jl:38-112) for many
     configurations at once: each keeps its own t, Δt and success counter, and
     all simulations still running advance together in one batched step.
+
+    ``lanes`` > 1 (without ``engine``) deals the simulations onto that many
+    engines, each advanced by its own host thread on its own CUDA stream: a
+    lane's Newton iterations do not wait for the slowest simulation of another
+    lane, and one lane's kernels run on the SMs that another lane's tail leaves
+    idle.  Each simulation takes the same steps as in a single batch, except
+    where the cost refactorisation rule's piggybacking (a batch-level choice of
+    when to refresh band factors) differs between the groupings; ``on_step``
+    is then called from the lane threads with each lane's engine and indices.
+    ``dirs`` overrides the per-simulation output directories.
 
     With params.output_dir set, VTK files are written as the reference does
     (run_simulation.jl:30-32, 86-90: the initial state, then after a converged
@@ -728,6 +822,8 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
     marks it.  A step whose norms are not finite (EB_SIM_NAN) counts as not
     converged, so it is rolled back and retried with half the Δt like any
     other failed step."""
+    if lanes > 1 and engine is None and len(confs) > 1:
+        return _run_lanes(confs, params, inters, max_steps, on_step, points_per_beam, dirs, lanes)
     eng = engine or GpuSimulations(confs, params, inters)
     p = params
     S = eng.n
@@ -742,7 +838,7 @@ def run_simulations(confs, params: SimulationParams, inters=None, max_steps: Opt
     tuned = False
     out = bool(p.output_dir)
     if out:
-        eng.vtk_open(output_dirs(p.output_dir, S), points_per_beam)
+        eng.vtk_open(dirs if dirs is not None else output_dirs(p.output_dir, S), points_per_beam)
         counter = np.zeros(S, np.int32)
         write_t = np.zeros(S)
         eng.vtk_write(counter, step, t)

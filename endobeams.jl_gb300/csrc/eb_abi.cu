@@ -274,11 +274,26 @@ struct PhaseTimer {
     phase_of[used] = phase;
     ++used;
   }
+  // While `ref` (the handle's timer-start event) is set, every phase interval is also kept as
+  // (phase, start, end) in ms from it, so that the intervals of handles stepped concurrently
+  // can be merged on one time axis.
+  cudaEvent_t ref = nullptr;
+  std::vector<float> iv;
+  void keep(int phase, cudaEvent_t a, cudaEvent_t b) {
+    if (!ref || iv.size() >= 3u * (1u << 20)) return;
+    float t0 = 0.f, t1 = 0.f;
+    if (cudaEventElapsedTime(&t0, ref, a) == cudaSuccess && cudaEventElapsedTime(&t1, ref, b) == cudaSuccess) {
+      iv.push_back((float)phase);
+      iv.push_back(t0);
+      iv.push_back(t1);
+    }
+  }
   void resolve() {  // call after the stream has been synchronised
     if (!on || used < 1) return;
     for (int i = 1; i < used; ++i) {
       float t = 0.f;
       if (cudaEventElapsedTime(&t, pool[i - 1], pool[i]) == cudaSuccess) ms[phase_of[i]] += t;
+      keep(phase_of[i], pool[i - 1], pool[i]);
     }
     std::swap(pool[0], pool[used - 1]);
     used = 1;
@@ -574,6 +589,7 @@ void resolve_graph_times(eb_handle* h, bool refactor) {
     float t = 0.f;
     if (cudaEventElapsedTime(&t, G.timer.pool[i - 1], G.timer.pool[i]) == cudaSuccess)
       h->timer.ms[G.timer.phase_of[i]] += t;
+    h->timer.keep(G.timer.phase_of[i], G.timer.pool[i - 1], G.timer.pool[i]);
   }
 }
 
@@ -1281,9 +1297,19 @@ int eb_set_device(int32_t device) {
   return EB_OK;
 }
 
+int eb_get_device(int32_t* device) {
+  if (!device) return fail(EB_ERR_ARG, "null device");
+  int d = 0;
+  CK(cudaGetDevice(&d));
+  *device = d;
+  return EB_OK;
+}
+
 int eb_timer_start(eb_handle* h) {
   if (!h) return fail(EB_ERR_ARG, "null handle");
   CK(cudaEventRecord(h->t0, h->stream));
+  h->timer.ref = h->timer.on ? h->t0 : nullptr;
+  h->timer.iv.clear();
   return EB_OK;
 }
 
@@ -1294,6 +1320,34 @@ int eb_timer_stop(eb_handle* h, double* ms) {
   float t = 0.f;
   CK(cudaEventElapsedTime(&t, h->t0, h->t1));
   *ms = t;
+  return EB_OK;
+}
+
+int eb_timer_between(eb_handle* from, eb_handle* to, double* ms) {
+  if (!from || !to || !ms) return fail(EB_ERR_ARG, "bad arguments");
+  CK(cudaEventSynchronize(to->t1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, from->t0, to->t1));
+  *ms = t;
+  return EB_OK;
+}
+
+int eb_get_phase_intervals(eb_handle* h, eb_handle* ref, int32_t phase, double* start_ms, double* end_ms,
+                           int64_t cap, int64_t* count) {
+  if (!h || !ref || !count || phase < 0 || phase >= EB_NPHASES || cap < 0 || (cap > 0 && (!start_ms || !end_ms)))
+    return fail(EB_ERR_ARG, "bad arguments");
+  float off = 0.f;
+  if (ref != h) CK(cudaEventElapsedTime(&off, ref->t0, h->t0));
+  int64_t n = 0;
+  for (size_t i = 0; i + 2 < h->timer.iv.size(); i += 3) {
+    if ((int)h->timer.iv[i] != phase) continue;
+    if (n < cap) {
+      start_ms[n] = (double)off + h->timer.iv[i + 1];
+      end_ms[n] = (double)off + h->timer.iv[i + 2];
+    }
+    ++n;
+  }
+  *count = n;
   return EB_OK;
 }
 

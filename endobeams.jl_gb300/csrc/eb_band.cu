@@ -1,4 +1,8 @@
 // Band assembly and blocked band LU (see eb_band.cuh).
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "eb_band.cuh"
 
 namespace eb {
@@ -198,11 +202,25 @@ __global__ void __launch_bounds__(kLuThreads) k_band_lu(Dev d, BandDev B) {
   }
 }
 
+cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> limit;  // (kernel, device) -> bytes set
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = limit[{func, dev}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 cudaError_t launch_band_lu(const Dev& d, const BandDev& B, int max_b, cudaStream_t s) {
   if (max_b <= 0) return cudaSuccess;
   // panel, U12 and 8 floats of padding for the unguarded reads past q
   const size_t smem = sizeof(float) * ((size_t)kPanel * (kPanel + 2 * (size_t)max_b) + 8);
-  cudaError_t e = cudaFuncSetAttribute(k_band_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void*)k_band_lu, smem);
   if (e != cudaSuccess) return e;
   k_band_lu<<<d.n_sims, kLuThreads, smem, s>>>(d, B);
   return cudaGetLastError();

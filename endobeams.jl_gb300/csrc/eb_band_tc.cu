@@ -330,7 +330,7 @@ size_t band_lu_tc_smem(int max_b) { return tc_smem_bytes(max_b); }
 cudaError_t launch_band_lu_tc(const Dev& d, const BandDev& B, int max_b, int* lu_fail, cudaStream_t s) {
   if (max_b <= 0) return cudaSuccess;
   const size_t smem = tc_smem_bytes(max_b);
-  cudaError_t e = cudaFuncSetAttribute(k_band_lu_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void*)k_band_lu_tc, smem);
   if (e != cudaSuccess) return e;
   k_band_lu_tc<<<d.n_sims, kTcThreads, smem, s>>>(d, B, lu_fail);
   return cudaGetLastError();

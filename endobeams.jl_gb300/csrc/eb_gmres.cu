@@ -418,10 +418,12 @@ cudaError_t launch_gmres(const SolverArgs& a, bool fp32, int threads, cudaStream
   cudaFuncSetAttribute(k_gmres<float>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   cudaFuncSetAttribute(k_gmres<double>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (fp32) {
-    cudaFuncSetAttribute(k_gmres<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void*)k_gmres<float>, smem);
+    if (e != cudaSuccess) return e;
     k_gmres<float><<<a.n_sims, threads, smem, s>>>(a);
   } else {
-    cudaFuncSetAttribute(k_gmres<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void*)k_gmres<double>, smem);
+    if (e != cudaSuccess) return e;
     k_gmres<double><<<a.n_sims, threads, smem, s>>>(a);
   }
   return cudaGetLastError();

@@ -94,6 +94,11 @@ constexpr int kMaxElemThreads = 256;  // largest block of the element and contac
 inline unsigned nblocks(int64_t n, int t = kThreads) { return (unsigned)((n + t - 1) / t); }
 
 // kernel launchers (eb_kernels.cu)
+// Raises `func`'s dynamic shared-memory limit on the current device to at least `bytes` and
+// never lowers it.  Handles stepped from several host threads launch the same kernel with
+// different sizes; a limit set for one launch must not undercut another thread's launch.
+cudaError_t raise_smem_limit(const void* func, size_t bytes);
+
 void launch_beam(const Dev& d, const Gauss3& g, cudaStream_t s);
 void launch_contact(const Dev& d, const Gauss3& g, cudaStream_t s);
 void launch_gather(const Dev& d, double alpha, bool with_contact, cudaStream_t s);

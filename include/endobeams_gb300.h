@@ -347,12 +347,19 @@ int eb_device_info(int32_t *count, char *name, int32_t name_len);
 /* Selects the CUDA device for handles created afterwards on this thread (no
  * reference counterpart: the reference has no device; one process per GPU). */
 int eb_set_device(int32_t device);
+/* The calling thread's current CUDA device (what a new host thread passes to
+ * eb_set_device before it steps handles created on this one). */
+int eb_get_device(int32_t *device);
 
 /* Device timing on the handle's stream (CUDA events; no reference counterpart,
  * the reference's equivalent is TimerOutputs, src/corrector.jl:7-42).
  * eb_timer_start/stop bracket any sequence of calls; stop returns elapsed ms. */
 int eb_timer_start(eb_handle *h);
 int eb_timer_stop(eb_handle *h, double *ms);
+/* Elapsed ms from `from`'s last eb_timer_start to `to`'s last eb_timer_stop: the
+ * device span of handles stepped concurrently (one host thread each, their own
+ * streams), measured between events of the two streams. */
+int eb_timer_between(eb_handle *from, eb_handle *to, double *ms);
 /* Per-phase device time (ms) and kernel-launch counts accumulated by eb_step
  * since the last reset (phases: EB_PHASE_*); needs eb_params.timing = 1 for
  * times, launch counts are always kept. */
@@ -366,6 +373,12 @@ int eb_timer_stop(eb_handle *h, double *ms);
 #define EB_PHASE_UPDATE 7
 #define EB_NPHASES 8
 int eb_get_phase_times(eb_handle *h, double *ms, int64_t *launches, int32_t reset);
+/* The phase's device intervals since h's last eb_timer_start (eb_params.timing = 1), in ms
+ * from ref's last eb_timer_start (ref may be h): `count` is the number of intervals, the
+ * first min(count, cap) are written.  Merged over handles stepped concurrently, they give
+ * the time during which any of them ran the phase. */
+int eb_get_phase_intervals(eb_handle *h, eb_handle *ref, int32_t phase, double *start_ms, double *end_ms,
+                           int64_t cap, int64_t *count);
 
 /* ---------------------------------------------------------------- learned Newton warm start
  * No reference counterpart: the reference starts every Newton loop from the

@@ -239,3 +239,22 @@ def test_single_simulation_abort_raises(eb):
                             max_timestep=0.02, simulation_end_time=0.1, max_iterations=20)
     res = api.run_simulations([None], p, engine=_ScriptedEngine([[21] * 20]))
     assert res.aborted == [True] and res.steps == [0]
+
+
+def test_lane_split_deals_by_size(eb):
+    """Lanes get the simulations round-robin in decreasing size (ties by index): every
+    simulation once, lane sizes within one of each other, and no more lanes than sims."""
+    sizes = [5, 40, 12, 40, 7, 3, 25]
+    parts = eb.api.lane_split(sizes, 3)
+    assert parts == [[1, 2, 5], [3, 4], [6, 0]]
+    assert sorted(i for p in parts for i in p) == list(range(len(sizes)))
+    assert eb.api.lane_split(sizes, 1) == [[1, 3, 6, 2, 4, 0, 5]]
+    assert len(eb.api.lane_split([1, 2], 8)) == 2
+
+
+def test_union_of_phase_intervals(eb):
+    u = eb.api.union_ms
+    assert u([]) == 0.0
+    assert u([np.array([[0.0, 2.0], [1.0, 3.0]]), np.array([[5.0, 6.0]])]) == 4.0
+    assert u([np.array([[0.0, 10.0]]), np.array([[1.0, 2.0], [3.0, 4.0]])]) == 10.0
+    assert u([np.array([[4.0, 5.0], [0.0, 1.0]])]) == 2.0
