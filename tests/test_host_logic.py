@@ -258,3 +258,49 @@ def test_union_of_phase_intervals(eb):
     assert u([np.array([[0.0, 2.0], [1.0, 3.0]]), np.array([[5.0, 6.0]])]) == 4.0
     assert u([np.array([[0.0, 10.0]]), np.array([[1.0, 2.0], [3.0, 4.0]])]) == 10.0
     assert u([np.array([[4.0, 5.0], [0.0, 1.0]])]) == 2.0
+
+
+class _ScriptedConf:
+    """A configuration stand-in for the lane tests: its element count and its k script."""
+
+    def __init__(self, n_elements, script):
+        self.beams = [None] * n_elements
+        self.script = list(script)
+
+
+def test_lanes_run_each_simulation_like_one_batch(eb, monkeypatch, tmp_path):
+    """run_simulations(lanes=3) on scripted engines: each lane gets its own engine and
+    thread, and every simulation takes the steps, k sequence and final time it takes in one
+    batch, with its output in its own sim_<index> directory."""
+    import threading
+    engines = []
+
+    def make(confs, params, inters):
+        e = _ScriptedEngine([c.script for c in confs])
+        e.thread = threading.current_thread().name
+        engines.append(e)
+        return e
+
+    monkeypatch.setattr(eb.api, "GpuSimulations", make)
+    monkeypatch.setattr(eb.api._lib, "current_device", lambda: 0)
+    monkeypatch.setattr(eb.api._lib, "set_device", lambda d: None)
+    scripts = [[3] * 40, [3, 21, 3] + [3] * 40, [9] * 5 + [3] * 40, [21, 21] + [3] * 40, [4] * 40]
+    sizes = [100, 400, 250, 50, 300]
+    p = eb.SimulationParams(alpha=-0.05, beta=0.28, gamma=0.55, initial_timestep=0.01, min_timestep=1e-4,
+                            max_timestep=0.02, simulation_end_time=0.1, max_iterations=20)
+    one = eb.run_simulations([_ScriptedConf(n, s) for n, s in zip(sizes, scripts)], p)
+    p.output_dir = str(tmp_path)
+    engines.clear()
+    three = eb.run_simulations([_ScriptedConf(n, s) for n, s in zip(sizes, scripts)], p, lanes=3)
+    assert len(engines) == 3 and len({e.thread for e in engines}) == 3
+    assert three.steps == one.steps and three.ks == one.ks and three.aborted == one.aborted
+    assert np.allclose(three.t, one.t, rtol=0, atol=1e-12)
+    # the lanes hold the simulations lane_split deals them and open those simulations' directories
+    parts = eb.api.lane_split(sizes, 3)
+    assert sorted(e.n for e in engines) == sorted(len(q) for q in parts)
+    for e in engines:
+        dirs = next(c[1] for c in e.calls if c[0] == "vtk_open")
+        lane = [int(d[-5:]) for d in dirs]
+        assert lane in parts
+    opened = sorted(d for e in engines for c in e.calls if c[0] == "vtk_open" for d in c[1])
+    assert opened == sorted(str(tmp_path / f"sim_{s:05d}") for s in range(5))
