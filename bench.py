@@ -857,8 +857,8 @@ def main():
         line = {"metric": METRIC if wl.kind == "stents" else "HHT steps/s (whole job), batched plain Newton",
                 "impl": "reference", "value": rate, "unit": "HHT steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": {"workload": wl.name, "sims": wl.count,
-                                                                "sample": len(idx)},
+                "dtype": "f64", "data": "synthetic",
+                "config": {"workload": wl.describe(0, 0, 0)["workload"], "sims": wl.count, "sample": len(idx)},
                 "cpu_baseline": {"value": rate, "unit": "HHT steps/s", "cores": cores, "kind": "port",
                                  "sample": sample},
                 "e2e": {"value": rate, "unit": "HHT steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
