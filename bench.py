@@ -53,6 +53,10 @@ sys.path.insert(0, ROOT)
 # SASS counters on a launch in which every element of a 48-wire stent is
 # evaluated.
 F_ELEM_FP64 = 1702.0 + 3085.0 + 2 * 5987.0
+# The algorithmic count of the same evaluation, from the oracle's restatement compiled over an
+# operation-counting double (oracle/flop_count.cpp, tests/test_flop_count.py): adds, multiplies,
+# divides and square roots of one undamped element (the stents' damping is zero).
+F_ELEM_ALGORITHMIC = 12153.0 + 14362.0 + 164.0 + 8.0
 
 # Bytes one contact-element evaluation must read: both node records (X0, u, u_dot, w_dot: 12
 # doubles; R, dR: 18) = 480 B, the element's R_e0, l0, radius (88 B), its index words (13 B)
@@ -638,7 +642,11 @@ def gpu_arm(args, rank, world):
         # FP64 flops of every element evaluation of the timed corrector iterations over the phase's device time
         avg_beam_ms = phase_ms["beam"] / launches["beam"]
         ach = F_ELEM_FP64 * tot["elem_evals"] / (dev_ms["beam"] * 1e-3) / 1e12
+        ach_alg = F_ELEM_ALGORITHMIC * tot["elem_evals"] / (dev_ms["beam"] * 1e-3) / 1e12
         rooflines["beam"] = {"kernel": "k_beam (corotational element, FP64)", "bound": "fp64", "achieved": ach,
+                             "algorithmic_flops_per_element": F_ELEM_ALGORITHMIC,
+                             "achieved_algorithmic": ach_alg,
+                             "executed_flops_per_element": F_ELEM_FP64,
                              "peak": peak_fp64, "peak_source": "measured (eb_fp64_peak FMA probe on this GPU)",
                              "unit": "TFLOP/s", "frac": ach / peak_fp64, "traffic": None,
                              "avg_launch_ms": avg_beam_ms, "share_of_step": phase_ms["beam"] / sum(phase_ms.values())}
