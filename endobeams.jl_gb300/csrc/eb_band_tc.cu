@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kTcThreads) k_band_lu_tc(Dev d, BandDev B, int
         phase[buf] ^= 1u;
         // this barrier also orders every thread's accumulator read of tile nc - 1 (same buffer
         // as tile nc + 1) before the MMAs of tile nc + 1 are issued; all threads get the same
-        // verdict from it, so they leave the loop together
+        // answer from it, so they leave the loop together
         umma::fence_before_sync();
         const int timed_out = __syncthreads_or(!done);
         umma::fence_after_sync();
